@@ -1,0 +1,212 @@
+/*
+ * tensormesh_gb300 -- C ABI of the GB300 (sm_103a) finite-element hot path.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (passed as void*, the caller's cudaStream_t), never allocates, never
+ * synchronises the stream (except where stated), and returns an int status:
+ *
+ *   TM_OK            0  success
+ *   TM_ERR_INVALID   1  bad argument (null pointer, unsupported combination)
+ *   TM_ERR_INDEX     2  an index or size out of range
+ *   TM_ERR_MAXITER   3  iterative solver hit its iteration cap
+ *   TM_ERR_BREAKDOWN 4  iterative solver breakdown (p^T A p <= 0, NaN)
+ *   TM_ERR_CUDA      5  a CUDA launch failed
+ *   TM_ERR_UNSUPPORTED 6 element/form/dtype combination not built
+ *   TM_ERR_TIMEOUT   7  a bounded device-side wait gave up
+ *
+ * Citations name the reference (TensorMesh) interface each entry replaces.
+ */
+#ifndef TENSORMESH_GB300_H
+#define TENSORMESH_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TM_OK 0
+#define TM_ERR_INVALID 1
+#define TM_ERR_INDEX 2
+#define TM_ERR_MAXITER 3
+#define TM_ERR_BREAKDOWN 4
+#define TM_ERR_CUDA 5
+#define TM_ERR_UNSUPPORTED 6
+#define TM_ERR_TIMEOUT 7
+
+/* element types: "triangle", "triangle6", "tetra", "tetra10" */
+#define TM_TRI3 0
+#define TM_TRI6 1
+#define TM_TET4 2
+#define TM_TET10 3
+
+/* integrands (assemble/builtin.py): Laplace gradu@gradv (62-63), mass u*v
+ * (100-101), isotropic linear elasticity Ba^T C Bb (173-179), load c*v /
+ * f(x)*v / f*v (886-969) */
+#define TM_FORM_LAPLACE 0
+#define TM_FORM_MASS 1
+#define TM_FORM_ELASTICITY 2
+#define TM_FORM_LOAD 3
+
+#define TM_F32 0
+#define TM_F64 1
+
+/* FP64 arithmetic: emulated double-float on the FP32 pipe (default) or
+ * native FP64 instructions (slow on GB300; kept as a cross-check). */
+#define TM_PREC_EMULATED 0
+#define TM_PREC_NATIVE 1
+
+/* where the coefficient of the integrand comes from */
+#define TM_COEF_SCALAR 0   /* scal[0..H-1]                          */
+#define TM_COEF_ELEMENT 1  /* coef[E]          (element_data)        */
+#define TM_COEF_POINT 2    /* coef[N*H]        (point_data, interpolated
+                              at quadrature points, node_assembler.py:389) */
+#define TM_COEF_QUAD 3     /* coef[E*Q*H]      (f(x_q) evaluated by caller) */
+
+/*
+ * Patch plan: the precomputed, mesh-only structure that replaces the
+ * reference's per-entry slot map ``elem_eids`` / ReduceProjector indices
+ * (assemble/element_assembler.py:838-875, assemble/projector.py:24-136,
+ * assemble/node_assembler.py:665-670).  Nodes are partitioned into patches;
+ * a patch owns a set of CSR rows and lists every element touching them.
+ * All arrays are device arrays.
+ *
+ *   vptr[P+1], vtx[]       local vertex table of each patch (global node ids)
+ *   eptr[P+1], elem[]      elements touching each patch (global ids, sorted)
+ *   econn[eptr[P]*B]       element connectivity in patch-local vertex ids
+ *   rptr[P+1], rows[]      owned rows of each patch (global node ids)
+ *   racc[]                 accumulator offset (in node slots) of each owned row
+ *   iptr[n_rows+1]         incidence range of each owned row (rows[] order)
+ *   inc_elem[], inc_a[]    incidence: patch-local element index, local vertex
+ *   inc_pos[n_inc*B]       position of column conn[e,b] inside row conn[e,a]
+ *   indptr[N+1]            node-level CSR row pointer (int64)
+ */
+typedef struct tm_patch_plan {
+  int32_t n_patches;
+  int32_t n_elements;
+  int32_t n_points;
+  int32_t n_basis;
+  const int32_t* vptr;
+  const int32_t* vtx;
+  const int32_t* eptr;
+  const int32_t* elem;
+  const uint16_t* econn;
+  const int32_t* rptr;
+  const int32_t* rows;
+  const int32_t* racc;
+  const int32_t* iptr;
+  const uint16_t* inc_elem;
+  const uint8_t* inc_a;
+  const uint8_t* inc_pos;
+  const int64_t* indptr;
+  int32_t max_vtx;    /* max local vertices of a patch */
+  int32_t max_slots;  /* max node slots owned by a patch */
+  int32_t max_rows;   /* max owned rows of a patch */
+  int32_t max_elems;  /* max elements touching a patch */
+} tm_patch_plan;
+
+typedef struct tm_assemble_args {
+  int32_t element;    /* TM_TRI3 ... */
+  int32_t form;       /* TM_FORM_* */
+  int32_t dtype;      /* TM_F32 / TM_F64: points, coef and output */
+  int32_t precision;  /* TM_PREC_* (TM_F64 only) */
+  int32_t coef_kind;  /* TM_COEF_* */
+  int32_t n_comp;     /* components of a load (H); 1 for bilinear forms */
+  int32_t n_quad;     /* quadrature points */
+  int32_t pad0;
+  const double* tables; /* w[Q], N[Q][B], dN[Q][B][D] (float64, device) */
+  const void* points;   /* [N][D] in dtype */
+  const void* coef;     /* see coef_kind, dtype */
+  double scal[3];       /* scalar coefficient(s) */
+  double lam;           /* elasticity: Lame lambda per unit coefficient */
+  double mu;            /* elasticity: Lame mu per unit coefficient */
+  void* out;            /* CSR values (dof level) or load vector [N*H] */
+} tm_assemble_args;
+
+/*
+ * Assemble a bilinear form straight into CSR values (canonical row/column
+ * order) or a linear form into a node vector.  Deterministic: the same
+ * inputs give bitwise-identical outputs on every run.
+ * Replaces ElementAssembler.__call__ (assemble/element_assembler.py:243-466)
+ * and NodeAssembler.__call__ (assemble/node_assembler.py:242-409) for the
+ * built-in forms, including the ReduceProjector scatter
+ * (assemble/projector.py:95-130).
+ */
+int tm_assemble(const tm_patch_plan* plan, const tm_assemble_args* args, void* stream);
+
+/*
+ * Backward (adjoint) assembly.  Given dL/d(values) of a tm_assemble call
+ * with the same plan and args, writes per-(patch, element) partial gradients:
+ *   pair_dX[n_pairs][B][D]          dL/dX of the element's nodes;
+ *   pair_dcoef: TM_COEF_ELEMENT [n_pairs], TM_COEF_POINT [n_pairs][B][C],
+ *               TM_COEF_QUAD [n_pairs][Q][C] (C = load components or 1).
+ * Either output may be NULL.  The partials of one element (or node) are
+ * summed in a fixed order with tm_segment_sum.  Replaces the reference's
+ * autograd through vmap/einsum/torch.inverse/index_add_
+ * (element/element.py:962-966, element/transformation.py:1289,
+ * assemble/projector.py:125).  FP64 runs native FP64 arithmetic.
+ */
+typedef struct tm_backward_args {
+  const void* grad_out; /* dL/d(values) [dof nnz] or dL/d(load) [N*H], dtype */
+  void* pair_dX;
+  void* pair_dcoef;
+} tm_backward_args;
+
+int tm_assemble_backward(const tm_patch_plan* plan, const tm_assemble_args* args, const tm_backward_args* bw,
+                         void* stream);
+
+/* dst[s][w] = sum_{k = ptr[s]}^{ptr[s+1]-1} src[perm[k]][w], in k order
+ * (deterministic segmented reduction). */
+int tm_segment_sum(int32_t dtype, int64_t n_segments, const int64_t* ptr, const int64_t* perm, int32_t width,
+                   const void* src, void* dst, void* stream);
+
+/*
+ * Physical coordinates of every quadrature point, out[E][Q][D] =
+ * sum_b N_b(xi_q) X[conn[e,b]] -- what the reference feeds to a ``func`` /
+ * ``x`` argument (assemble/node_assembler.py:389, element_assembler.py:440).
+ */
+int tm_quadrature_points(int32_t element, int32_t dtype, int32_t n_quad, const double* tables,
+                         const void* points, const int32_t* elements, int64_t n_elements,
+                         void* out, void* stream);
+
+/* y = A x for CSR A (replaces SparseMatrix @ / spmv, sparse/mm/__init__.py:
+ * 22-72).  dtype applies to values, x and y. */
+int tm_spmv_csr(int32_t dtype, int64_t n_rows, const int64_t* indptr, const int32_t* indices,
+                const void* values, const void* x, void* y, void* stream);
+
+/*
+ * Jacobi-preconditioned CG, whole iteration in one cooperative launch.
+ * Replaces K.solve for SPD systems (torch_sla SparseTensor.solve; in-repo
+ * equivalents sparse/solve/torch_solve.py:24-59 Jacobi, 70-128 cg_py,
+ * 130-248 bicgstab_py).  Stops when ||r|| <= max(rtol*||b||, atol) on the
+ * recurrence residual or after maxiter iterations.  x holds the initial guess
+ * on entry.  work: caller-owned device scratch of at least
+ * tm_pcg_workspace_bytes(dtype, n, tm_pcg_max_blocks(dtype)) bytes.
+ * Statuses of the solve itself are read back with tm_pcg_result.
+ */
+int64_t tm_pcg_workspace_bytes(int32_t dtype, int64_t n, int32_t max_blocks);
+int tm_pcg_max_blocks(int32_t dtype);
+int tm_pcg_jacobi(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
+                  const void* values, const void* b, void* x, double rtol, double atol, int32_t maxiter,
+                  void* work, int64_t work_bytes, void* stream);
+/* Synchronises the stream; returns the solve status (TM_OK, TM_ERR_MAXITER,
+ * TM_ERR_BREAKDOWN, TM_ERR_TIMEOUT) and its iteration count / residuals. */
+int tm_pcg_result(const void* work, int32_t* iters, double* res, double* bnorm, void* stream);
+
+/* 1/diag(A) with missing diagonals taken as 1 (torch_solve.py:24-59). */
+int tm_csr_diagonal_inverse(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
+                            const void* values, void* out, void* stream);
+
+/* dst[i] = src[map[i]] and dst[map[i]] = src[i]: the value compaction and
+ * recovery of static condensation (operator/condense.py:294-299, 429-458). */
+int tm_gather(int32_t dtype, int64_t n, const int64_t* map, const void* src, void* dst, void* stream);
+int tm_scatter(int32_t dtype, int64_t n, const int64_t* map, const void* src, void* dst, void* stream);
+
+/* f_i = rhs[inner_dof] - K_io u_o (operator/condense.py:300-309, 388-427). */
+int tm_condense_rhs(int32_t dtype, int64_t n_inner, const int64_t* inner_dof, const void* rhs,
+                    const int64_t* io_indptr, const int32_t* io_indices, const void* io_values,
+                    const void* u_outer, void* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

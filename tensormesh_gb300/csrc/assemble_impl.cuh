@@ -1,0 +1,371 @@
+// Patch-based deterministic assembly (generic over element, form and
+// arithmetic).  One CTA per patch:
+//
+//   phase 0  gather the patch's vertex coordinates (and point data) into
+//            shared memory, converted once to the compute type R;
+//   phase A  element-parallel: each thread computes the full element matrix
+//            (or load vector) of one element into a shared staging slot --
+//            Jacobian, |det J|, physical gradients and the quadrature sum
+//            all stay in registers/shared memory;
+//   phase B  row-parallel: the thread that owns a CSR row walks that row's
+//            incidences (element, local vertex a) in a fixed order and adds
+//            stage[e][a][b] into the row's accumulator at the precomputed
+//            position of column conn[e][b];
+//   write    warp-per-row copy of the finished rows into the canonical CSR
+//            value array (each value written exactly once, no atomics).
+//
+// The accumulation order of every CSR value is fixed by the plan, so the
+// result is bitwise reproducible run to run.  This replaces the reference's
+// vmap/einsum element integrals (assemble/element_assembler.py:402-464,
+// element/element.py:874-968, element/transformation.py:1236-1293) and the
+// index_add_ scatter (assemble/projector.py:95-130).
+#pragma once
+#include "tm_common.cuh"
+#include "../../include/tensormesh_gb300.h"
+
+namespace tmg {
+
+template <int EL> struct Elem;
+template <> struct Elem<TM_TRI3> { static constexpr int D = 2, B = 3; };
+template <> struct Elem<TM_TRI6> { static constexpr int D = 2, B = 6; };
+template <> struct Elem<TM_TET4> { static constexpr int D = 3, B = 4; };
+template <> struct Elem<TM_TET10> { static constexpr int D = 3, B = 10; };
+
+constexpr int kThreads = 256;
+constexpr int kMaxQuad = 11;
+
+template <int EL, int FORM, int H>
+struct Layout {
+  static constexpr int D = Elem<EL>::D, B = Elem<EL>::B;
+  static constexpr bool kLoad = FORM == TM_FORM_LOAD;
+  // staged entries per element
+  static constexpr int SE = kLoad ? B * H : B * B * H * H;
+  // accumulator entries per node slot (bilinear) or per owned row (load)
+  static constexpr int HH = kLoad ? H : H * H;
+};
+
+template <class R>
+TM_D R tm_fma_acc(R acc, R a, R b) { return acc + a * b; }
+
+// Inverse-transpose data of one quadrature point: physical gradients and JxW.
+template <int D, int B, class R>
+TM_D void point_geometry(const R (&X)[B][D], const R* dNq /*[B][D]*/, R wq, R (&g)[B][D], R& jxw) {
+  // J[i][j] = sum_b X[b][j] dN[b][i]   (element.py:962, J = dx_j / dxi_i)
+  R J[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      R s = Num<R>::zero();
+#pragma unroll
+      for (int b = 0; b < B; ++b) s = tm_fma_acc(s, X[b][j], dNq[b * D + i]);
+      J[i][j] = s;
+    }
+  R inv[D][D];  // adjugate; divided by det below
+  R det;
+  if constexpr (D == 2) {
+    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    inv[0][0] = J[1][1];
+    inv[0][1] = -J[0][1];
+    inv[1][0] = -J[1][0];
+    inv[1][1] = J[0][0];
+  } else {
+    inv[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    inv[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+    inv[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+    inv[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    inv[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+    inv[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+    inv[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    inv[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+    inv[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    det = J[0][0] * inv[0][0] + J[0][1] * inv[1][0] + J[0][2] * inv[2][0];
+  }
+  R rdet = Num<R>::from_float(1.f) / det;
+  // grad[b][j] = sum_i dN[b][i] Jinv[j][i]  (element.py:966)
+#pragma unroll
+  for (int b = 0; b < B; ++b)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      R s = Num<R>::zero();
+#pragma unroll
+      for (int i = 0; i < D; ++i) s = tm_fma_acc(s, dNq[b * D + i], inv[j][i]);
+      g[b][j] = s * rdet;
+    }
+  jxw = wq * Num<R>::abs(det);  // transformation.py:1289
+}
+
+template <int EL, int FORM, int H, class T, class R>
+__global__ void __launch_bounds__(kThreads)
+patch_assemble_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
+  using L = Layout<EL, FORM, H>;
+  constexpr int D = L::D, B = L::B, SE = L::SE, HH = L::HH;
+  const int p = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int Q = args.n_quad;
+
+  const int vbeg = plan.vptr[p], nv = plan.vptr[p + 1] - vbeg;
+  const int ebeg = plan.eptr[p], ne = plan.eptr[p + 1] - ebeg;
+  const int rbeg = plan.rptr[p], nr = plan.rptr[p + 1] - rbeg;
+  if (nr == 0) return;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* s_tab = reinterpret_cast<R*>(smem_raw);                  // w, N, dN
+  R* s_w = s_tab;
+  R* s_N = s_w + kMaxQuad;
+  R* s_dN = s_N + kMaxQuad * B;
+  R* s_X = s_dN + kMaxQuad * B * D;                           // [max_vtx][D]
+  R* s_pc = s_X + plan.max_vtx * D;                           // [max_vtx][H] point coef
+  const int pc_len = (args.coef_kind == TM_COEF_POINT) ? plan.max_vtx * (L::kLoad ? H : 1) : 0;
+  R* s_acc = s_pc + pc_len;
+  const int acc_len = L::kLoad ? plan.max_rows * H : plan.max_slots * HH;
+  R* s_stage = s_acc + acc_len;
+  int* s_cur = reinterpret_cast<int*>(s_stage + chunk * SE);
+
+  // --- phase 0: tables, coordinates, point data, zero accumulators -------
+  for (int i = tid; i < Q; i += kThreads) s_w[i] = Num<R>::from_double(args.tables[i]);
+  for (int i = tid; i < Q * B; i += kThreads) s_N[i] = Num<R>::from_double(args.tables[Q + i]);
+  for (int i = tid; i < Q * B * D; i += kThreads) s_dN[i] = Num<R>::from_double(args.tables[Q + Q * B + i]);
+  const T* pts = static_cast<const T*>(args.points);
+  for (int i = tid; i < nv * D; i += kThreads) {
+    int v = plan.vtx[vbeg + i / D];
+    s_X[i] = tm_load<R, T>(pts[(int64_t)v * D + i % D]);
+  }
+  if (args.coef_kind == TM_COEF_POINT) {
+    constexpr int PC = L::kLoad ? H : 1;
+    const T* pc = static_cast<const T*>(args.coef);
+    for (int i = tid; i < nv * PC; i += kThreads) {
+      int v = plan.vtx[vbeg + i / PC];
+      s_pc[i] = tm_load<R, T>(pc[(int64_t)v * PC + i % PC]);
+    }
+  }
+  const int nacc = L::kLoad ? nr * H : 0;
+  {
+    int total = L::kLoad ? nacc : 0;
+    if (!L::kLoad) {
+      // owned node slots of this patch = racc of last row + its degree
+      int lr = rbeg + nr - 1;
+      int r = plan.rows[lr];
+      total = (plan.racc[lr] + (int)(plan.indptr[r + 1] - plan.indptr[r])) * HH;
+    }
+    for (int i = tid; i < total; i += kThreads) s_acc[i] = Num<R>::zero();
+  }
+  for (int i = tid; i < nr; i += kThreads) s_cur[i] = plan.iptr[rbeg + i];
+  __syncthreads();
+
+  R scal[3];
+#pragma unroll
+  for (int h = 0; h < 3; ++h) scal[h] = Num<R>::from_double(args.scal[h]);
+  // Lame constants per unit coefficient (functional/elasticity.py:202-284)
+  const R lam1 = Num<R>::from_double(args.lam);
+  const R mu1 = Num<R>::from_double(args.mu);
+  const T* coef = static_cast<const T*>(args.coef);
+
+  for (int cbeg = 0; cbeg < ne; cbeg += chunk) {
+    const int cend = min(ne, cbeg + chunk);
+    // --- phase A: element matrices into the staging area --------------------
+    for (int le = cbeg + tid; le < cend; le += kThreads) {
+      const int e = plan.elem[ebeg + le];
+      int lv[B];
+      R X[B][D];
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        lv[b] = plan.econn[(int64_t)(ebeg + le) * B + b];
+#pragma unroll
+        for (int d = 0; d < D; ++d) X[b][d] = s_X[lv[b] * D + d];
+      }
+      R ce = scal[0];
+      if (args.coef_kind == TM_COEF_ELEMENT) ce = tm_load<R, T>(coef[e]);
+      R* Ke = s_stage + (le - cbeg) * SE;
+      for (int i = 0; i < SE; ++i) Ke[i] = Num<R>::zero();
+      for (int q = 0; q < Q; ++q) {
+        R g[B][D], jxw;
+        point_geometry<D, B, R>(X, s_dN + q * B * D, s_w[q], g, jxw);
+        const R* Nq = s_N + q * B;
+        if constexpr (FORM == TM_FORM_LOAD) {
+          R fq[H];
+#pragma unroll
+          for (int h = 0; h < H; ++h) {
+            if (args.coef_kind == TM_COEF_SCALAR) fq[h] = scal[h];
+            else if (args.coef_kind == TM_COEF_ELEMENT) fq[h] = ce;
+            else if (args.coef_kind == TM_COEF_QUAD) fq[h] = tm_load<R, T>(coef[((int64_t)e * Q + q) * H + h]);
+            else {
+              R s = Num<R>::zero();
+#pragma unroll
+              for (int b = 0; b < B; ++b) s = tm_fma_acc(s, s_pc[lv[b] * H + h], Nq[b]);
+              fq[h] = s;
+            }
+            fq[h] = fq[h] * jxw;
+          }
+#pragma unroll
+          for (int i = 0; i < B; ++i)
+#pragma unroll
+            for (int h = 0; h < H; ++h) Ke[i * H + h] = tm_fma_acc(Ke[i * H + h], fq[h], Nq[i]);
+        } else {
+          R cq = ce;
+          if (args.coef_kind == TM_COEF_POINT) {
+            R s = Num<R>::zero();
+#pragma unroll
+            for (int b = 0; b < B; ++b) s = tm_fma_acc(s, s_pc[lv[b]], Nq[b]);
+            cq = s;
+          } else if (args.coef_kind == TM_COEF_QUAD) {
+            cq = tm_load<R, T>(coef[(int64_t)e * Q + q]);
+          }
+          const R cw = cq * jxw;
+          if constexpr (FORM == TM_FORM_LAPLACE) {
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+              for (int j = 0; j < B; ++j) {
+                R dot = Num<R>::zero();
+#pragma unroll
+                for (int d = 0; d < D; ++d) dot = tm_fma_acc(dot, g[i][d], g[j][d]);
+                Ke[i * B + j] = tm_fma_acc(Ke[i * B + j], cw, dot);
+              }
+          } else if constexpr (FORM == TM_FORM_MASS) {
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+              for (int j = 0; j < B; ++j) Ke[i * B + j] = tm_fma_acc(Ke[i * B + j], cw, Nq[i] * Nq[j]);
+          } else {  // elasticity: lam g_i[a] g_j[b] + mu (delta_ab g_i.g_j + g_i[b] g_j[a])
+            const R lw = cw * lam1, mw = cw * mu1;
+#pragma unroll
+            for (int i = 0; i < B; ++i)
+#pragma unroll
+              for (int j = 0; j < B; ++j) {
+                R dot = Num<R>::zero();
+#pragma unroll
+                for (int d = 0; d < D; ++d) dot = tm_fma_acc(dot, g[i][d], g[j][d]);
+                R* blk = Ke + (i * B + j) * HH;
+#pragma unroll
+                for (int a = 0; a < H; ++a)
+#pragma unroll
+                  for (int b = 0; b < H; ++b) {
+                    R v = lw * (g[i][a] * g[j][b]) + mw * (g[i][b] * g[j][a]);
+                    if (a == b) v = v + mw * dot;
+                    blk[a * H + b] = blk[a * H + b] + v;
+                  }
+              }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // --- phase B: row-owner gather in incidence order ------------------------
+    for (int lr = tid; lr < nr; lr += kThreads) {
+      int cur = s_cur[lr];
+      const int end = plan.iptr[rbeg + lr + 1];
+      const int ro = L::kLoad ? lr * H : plan.racc[rbeg + lr] * HH;
+      while (cur < end) {
+        const int le = plan.inc_elem[cur];
+        if (le >= cend) break;
+        const int a = plan.inc_a[cur];
+        const R* Ke = s_stage + (le - cbeg) * SE;
+        if constexpr (L::kLoad) {
+#pragma unroll
+          for (int h = 0; h < H; ++h) s_acc[ro + h] = s_acc[ro + h] + Ke[a * H + h];
+        } else {
+#pragma unroll
+          for (int b = 0; b < B; ++b) {
+            const int pos = plan.inc_pos[(int64_t)cur * B + b];
+            R* dst = s_acc + ro + pos * HH;
+            const R* src = Ke + (a * B + b) * HH;
+#pragma unroll
+            for (int t = 0; t < HH; ++t) dst[t] = dst[t] + src[t];
+          }
+        }
+        ++cur;
+      }
+      s_cur[lr] = cur;
+    }
+    __syncthreads();
+  }
+
+  // --- write the finished rows -----------------------------------------------
+  T* out = static_cast<T*>(args.out);
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int lr = warp; lr < nr; lr += kThreads / 32) {
+    const int r = plan.rows[rbeg + lr];
+    if constexpr (L::kLoad) {
+      if (lane < H) out[(int64_t)r * H + lane] = tm_store<T, R>(s_acc[lr * H + lane]);
+    } else {
+      const int64_t s0 = plan.indptr[r];
+      const int deg = (int)(plan.indptr[r + 1] - s0);
+      const int ro = plan.racc[rbeg + lr];
+      if constexpr (H == 1) {
+        for (int k = lane; k < deg; k += 32) out[s0 + k] = tm_store<T, R>(s_acc[ro + k]);
+      } else {
+#pragma unroll
+        for (int a = 0; a < H; ++a) {
+          const int64_t base = (int64_t)HH * s0 + (int64_t)a * H * deg;
+          for (int t = lane; t < deg * H; t += 32) {
+            const int k = t / H, b = t - (t / H) * H;
+            out[base + t] = tm_store<T, R>(s_acc[(ro + k) * HH + a * H + b]);
+          }
+        }
+      }
+    }
+  }
+}
+
+// Shared-memory bytes needed by one CTA.
+template <int EL, int FORM, int H, class R>
+inline size_t patch_smem_bytes(const tm_patch_plan& plan, int coef_kind, int chunk) {
+  using L = Layout<EL, FORM, H>;
+  constexpr int D = L::D, B = L::B;
+  size_t n = kMaxQuad + kMaxQuad * B + kMaxQuad * B * D + (size_t)plan.max_vtx * D;
+  if (coef_kind == TM_COEF_POINT) n += (size_t)plan.max_vtx * (L::kLoad ? H : 1);
+  n += L::kLoad ? (size_t)plan.max_rows * H : (size_t)plan.max_slots * L::HH;
+  n += (size_t)chunk * L::SE;
+  return n * sizeof(R) + (size_t)plan.max_rows * sizeof(int) + 16;
+}
+
+template <int EL, int FORM, int H, class T, class R>
+int launch_patch_assemble(const tm_patch_plan& plan, const tm_assemble_args& args, cudaStream_t stream) {
+  using L = Layout<EL, FORM, H>;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int max_optin = 0;
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  // staging chunk: as many elements as threads, shrunk to fit shared memory
+  int chunk = kThreads;
+  size_t bytes = patch_smem_bytes<EL, FORM, H, R>(plan, args.coef_kind, chunk);
+  while (bytes > (size_t)max_optin && chunk > 1) {
+    chunk = chunk / 2;
+    bytes = patch_smem_bytes<EL, FORM, H, R>(plan, args.coef_kind, chunk);
+  }
+  if (bytes > (size_t)max_optin) return TM_ERR_INDEX;
+  auto kern = patch_assemble_kernel<EL, FORM, H, T, R>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+    return TM_ERR_CUDA;
+  kern<<<plan.n_patches, kThreads, bytes, stream>>>(plan, args, chunk);
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+// Dispatch over form/H/precision for one element type (instantiated in one
+// translation unit per element so the build parallelises).
+template <int EL>
+int assemble_element(const tm_patch_plan& plan, const tm_assemble_args& a, cudaStream_t s) {
+  constexpr int D = Elem<EL>::D;
+#define TM_PREC_DISPATCH(FORM, H)                                                         \
+  do {                                                                                    \
+    if (a.dtype == TM_F32) return launch_patch_assemble<EL, FORM, H, float, float>(plan, a, s); \
+    if (a.precision == TM_PREC_NATIVE)                                                    \
+      return launch_patch_assemble<EL, FORM, H, double, double>(plan, a, s);             \
+    return launch_patch_assemble<EL, FORM, H, double, df64>(plan, a, s);                 \
+  } while (0)
+  switch (a.form) {
+    case TM_FORM_LAPLACE: TM_PREC_DISPATCH(TM_FORM_LAPLACE, 1);
+    case TM_FORM_MASS: TM_PREC_DISPATCH(TM_FORM_MASS, 1);
+    case TM_FORM_ELASTICITY: TM_PREC_DISPATCH(TM_FORM_ELASTICITY, D);
+    case TM_FORM_LOAD:
+      if (a.n_comp == 1) TM_PREC_DISPATCH(TM_FORM_LOAD, 1);
+      if (a.n_comp == 2) TM_PREC_DISPATCH(TM_FORM_LOAD, 2);
+      if (a.n_comp == 3) TM_PREC_DISPATCH(TM_FORM_LOAD, 3);
+      return TM_ERR_UNSUPPORTED;
+    default: return TM_ERR_UNSUPPORTED;
+  }
+#undef TM_PREC_DISPATCH
+}
+
+}  // namespace tmg

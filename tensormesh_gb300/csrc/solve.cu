@@ -1,0 +1,394 @@
+// Jacobi-preconditioned CG as one cooperative persistent kernel, plus the
+// small CSR kernels around it (diagonal, gathers for static condensation).
+//
+// Replaces K.solve for SPD systems: the reference's Jacobi preconditioner
+// (sparse/solve/torch_solve.py:24-59) inside a CG loop that it runs as one
+// PyTorch launch per vector op (torch_solve.py:70-128, 130-248).  Here the
+// whole iteration lives in one launch:
+//   * rows are split into contiguous ranges, one per CTA;
+//   * p is double-buffered, and the SpMV forms p_new = z + beta p_old for the
+//     columns it gathers, so an iteration needs two grid barriers (after
+//     p.Ap and after r.z);
+//   * dot products reduce per CTA, then every CTA sums the per-CTA partials
+//     in the same order -- deterministic, no atomics on values;
+//   * the grid barrier is a counter + generation word with a bounded wait:
+//     after ~1 s it raises TM_ERR_TIMEOUT and every CTA returns.
+#include "tm_common.cuh"
+#include "../../include/tensormesh_gb300.h"
+
+namespace tmg {
+
+constexpr int kPcgThreads = 512;
+constexpr int kGroup = 8;  // lanes per CSR row
+
+struct PcgState {
+  unsigned int count;
+  unsigned int gen;
+  int status;
+  int iters;
+  double res;   // final recurrence residual norm
+  double bnorm;
+};
+
+__device__ __forceinline__ bool grid_sync(PcgState* st, unsigned nblocks, unsigned& my_gen) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned g = my_gen;
+    __threadfence();
+    unsigned arrived = atomicAdd(&st->count, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(&st->count, 0u);
+      __threadfence();
+      atomicAdd(&st->gen, 1u);
+    } else {
+      volatile unsigned* gen = &st->gen;
+      long long spins = 0;
+      while (*gen == g) {
+        if (++spins > (1ll << 25)) {  // ~1 s with the 32 ns back-off
+          atomicExch(&st->status, TM_ERR_TIMEOUT);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  ++my_gen;
+  __syncthreads();
+  return *((volatile int*)&st->status) == TM_OK;
+}
+
+template <class T>
+__device__ __forceinline__ T block_sum(T v, T* s_red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) s_red[warp] = v;
+  __syncthreads();
+  T t = 0;
+  if (warp == 0) {
+    t = lane < (blockDim.x >> 5) ? s_red[lane] : T(0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;  // valid in thread 0
+}
+
+// Sum the per-CTA partials (same order in every CTA).
+template <class T>
+__device__ __forceinline__ T sum_partials(const T* part, int n, T* s_red) {
+  T v = 0;
+  if (threadIdx.x < 32) {
+    for (int i = threadIdx.x; i < n; i += 32) v += ((volatile T*)part)[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) s_red[0] = v;
+  }
+  __syncthreads();
+  T r = s_red[0];
+  __syncthreads();
+  return r;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPcgThreads)
+pcg_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ idx,
+           const T* __restrict__ val, const T* __restrict__ dinv, const T* __restrict__ b, T* __restrict__ x,
+           T* r, T* z, T* p0, T* p1, T* q, T* partials, PcgState* st, double rtol, double atol, int maxiter) {
+  __shared__ T s_red[32];
+  const unsigned nb = gridDim.x;
+  unsigned my_gen = 0;
+  // my_gen must start at the value of st->gen at launch: the host zeroes it.
+  const int64_t rows_per = (n + nb - 1) / nb;
+  const int64_t r0 = min(n, (int64_t)blockIdx.x * rows_per), r1 = min(n, r0 + rows_per);
+  const int g = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int ngroups = kPcgThreads / kGroup;
+  T* partA = partials;
+  T* partB = partials + nb;
+  T* partC = partials + 2 * nb;
+
+  // r = b - A x ; z = D^-1 r ; p = z ; partial rz, rr, bb
+  T rz_l = 0, rr_l = 0, bb_l = 0;
+  for (int64_t row = r0 + g; row < r1; row += ngroups) {
+    T s = 0;
+    for (int64_t k = indptr[row] + lane; k < indptr[row + 1]; k += kGroup) s += val[k] * x[idx[k]];
+#pragma unroll
+    for (int o = kGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kGroup);
+    if (lane == 0) {
+      T rv = b[row] - s;
+      T zv = dinv[row] * rv;
+      r[row] = rv;
+      z[row] = zv;
+      p0[row] = zv;
+      rz_l += rv * zv;
+      rr_l += rv * rv;
+      bb_l += b[row] * b[row];
+    }
+  }
+  T t = block_sum(rz_l, s_red);
+  if (threadIdx.x == 0) partA[blockIdx.x] = t;
+  t = block_sum(rr_l, s_red);
+  if (threadIdx.x == 0) partB[blockIdx.x] = t;
+  t = block_sum(bb_l, s_red);
+  if (threadIdx.x == 0) partC[blockIdx.x] = t;
+  if (!grid_sync(st, nb, my_gen)) return;
+  T rz = sum_partials(partA, nb, s_red);
+  T rr = sum_partials(partB, nb, s_red);
+  const T bb = sum_partials(partC, nb, s_red);
+  const double bnorm = sqrt((double)bb);
+  const double tol = fmax(rtol * bnorm, atol);
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->bnorm = bnorm;
+  if (!grid_sync(st, nb, my_gen)) return;  // partial buffers are reused below
+
+  T beta = 0;
+  T* pold = p0;  // p of the previous iteration (p0 holds z for it=0 with beta=0)
+  T* pnew = p1;
+  int it = 0;
+  int status = TM_ERR_MAXITER;
+  for (; it <= maxiter; ++it) {
+    if (sqrt((double)rr) <= tol) {
+      status = TM_OK;
+      break;
+    }
+    if (it == maxiter) break;
+    // q = A p_new, p_new = z + beta p_old formed on the fly; partial p.q
+    T pq_l = 0;
+    for (int64_t row = r0 + g; row < r1; row += ngroups) {
+      T s = 0;
+      for (int64_t k = indptr[row] + lane; k < indptr[row + 1]; k += kGroup) {
+        const int c = idx[k];
+        s += val[k] * (z[c] + beta * pold[c]);
+      }
+#pragma unroll
+      for (int o = kGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kGroup);
+      if (lane == 0) {
+        T pv = z[row] + beta * pold[row];
+        q[row] = s;
+        pq_l += pv * s;
+      }
+    }
+    t = block_sum(pq_l, s_red);
+    if (threadIdx.x == 0) partA[blockIdx.x] = t;
+    if (!grid_sync(st, nb, my_gen)) return;
+    const T pq = sum_partials(partA, nb, s_red);
+    if (!(pq > T(0))) {
+      status = TM_ERR_BREAKDOWN;
+      break;
+    }
+    const T alpha = rz / pq;
+    T rz_n = 0, rr_n = 0;
+    // every row of p_new is written here by its owner (rows were read as
+    // z + beta*pold above, which this CTA's rows still hold in z/pold)
+    for (int64_t row = r0 + threadIdx.x; row < r1; row += kPcgThreads) {
+      T pv = z[row] + beta * pold[row];
+      pnew[row] = pv;
+      x[row] += alpha * pv;
+      T rv = r[row] - alpha * q[row];
+      r[row] = rv;
+      T zv = dinv[row] * rv;
+      z[row] = zv;
+      rz_n += rv * zv;
+      rr_n += rv * rv;
+    }
+    t = block_sum(rz_n, s_red);
+    if (threadIdx.x == 0) partB[blockIdx.x] = t;
+    t = block_sum(rr_n, s_red);
+    if (threadIdx.x == 0) partC[blockIdx.x] = t;
+    if (!grid_sync(st, nb, my_gen)) return;
+    const T rzn = sum_partials(partB, nb, s_red);
+    rr = sum_partials(partC, nb, s_red);
+    beta = rzn / rz;
+    rz = rzn;
+    T* tmp = pold;
+    pold = pnew;
+    pnew = tmp;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->iters = it;
+    st->res = sqrt((double)rr);
+    atomicCAS(&st->status, TM_OK, status);
+  }
+}
+
+template <class T>
+__global__ void diag_inv_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ idx,
+                                const T* __restrict__ val, T* __restrict__ dinv) {
+  int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  int64_t lo = indptr[row], hi = indptr[row + 1];
+  T d = T(1);  // missing diagonal -> 1 (torch_solve.py:24-49, at_least=1)
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    int c = idx[mid];
+    if (c == row) {
+      d = val[mid];
+      break;
+    }
+    if (c < row) lo = mid + 1; else hi = mid;
+  }
+  dinv[row] = d != T(0) ? T(1) / d : T(1);
+}
+
+template <class T>
+__global__ void gather_kernel(int64_t n, const int64_t* __restrict__ map, const T* __restrict__ src, T* __restrict__ dst) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[map[i]];
+}
+
+// f_i = rhs[inner_dof[i]] - sum_{k in row i of K_io} K_io[k] * u_o[col[k]]
+template <class T>
+__global__ void condense_rhs_kernel(int64_t n_inner, const int64_t* __restrict__ inner_dof, const T* __restrict__ rhs,
+                                    const int64_t* __restrict__ io_ptr, const int32_t* __restrict__ io_idx,
+                                    const T* __restrict__ io_val, const T* __restrict__ u_o, T* __restrict__ out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n_inner) return;
+  T s = 0;
+  for (int64_t k = io_ptr[i]; k < io_ptr[i + 1]; ++k) s += io_val[k] * u_o[io_idx[k]];
+  out[i] = rhs[inner_dof[i]] - s;
+}
+
+template <class T>
+__global__ void scatter_kernel(int64_t n, const int64_t* __restrict__ map, const T* __restrict__ src, T* __restrict__ dst) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[map[i]] = src[i];
+}
+
+}  // namespace tmg
+
+extern "C" int64_t tm_pcg_workspace_bytes(int32_t dtype, int64_t n, int32_t max_blocks) {
+  const int64_t es = dtype == TM_F64 ? 8 : 4;
+  // state (256 B) | dinv r z p0 p1 q (6n) | partials (3 * blocks)
+  return 256 + es * (6 * n + 3 * (int64_t)max_blocks);
+}
+
+extern "C" int tm_pcg_max_blocks(int32_t dtype) {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (dtype == TM_F64)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tmg::pcg_kernel<double>, tmg::kPcgThreads, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tmg::pcg_kernel<float>, tmg::kPcgThreads, 0);
+  return sms * (per_sm > 2 ? 2 : per_sm);
+}
+
+template <class T>
+static int launch_pcg(int64_t n, const int64_t* indptr, const int32_t* indices, const T* values, const T* b, T* x,
+                      double rtol, double atol, int maxiter, char* w, int nb, cudaStream_t s) {
+  tmg::PcgState* st = reinterpret_cast<tmg::PcgState*>(w);
+  T* base = reinterpret_cast<T*>(w + 256);
+  T* dinv = base;
+  T* r = base + n;
+  T* z = base + 2 * n;
+  T* p0 = base + 3 * n;
+  T* p1 = base + 4 * n;
+  T* q = base + 5 * n;
+  T* partials = base + 6 * n;
+  if (cudaMemsetAsync(st, 0, sizeof(tmg::PcgState), s) != cudaSuccess) return TM_ERR_CUDA;
+  tmg::diag_inv_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, indptr, indices, values, dinv);
+  const T* cdinv = dinv;
+  void* args[] = {(void*)&n, (void*)&indptr, (void*)&indices, (void*)&values, (void*)&cdinv, (void*)&b, (void*)&x,
+                  (void*)&r, (void*)&z, (void*)&p0, (void*)&p1, (void*)&q, (void*)&partials, (void*)&st,
+                  (void*)&rtol, (void*)&atol, (void*)&maxiter};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)tmg::pcg_kernel<T>, dim3(nb), dim3(tmg::kPcgThreads), args,
+                                              0, s);
+  return e == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+extern "C" int tm_pcg_jacobi(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
+                             const void* values, const void* b, void* x, double rtol, double atol, int32_t maxiter,
+                             void* work, int64_t work_bytes, void* stream) {
+  if (n < 0 || maxiter < 0) return TM_ERR_INVALID;
+  if (n == 0) return TM_OK;
+  if (!indptr || !indices || !values || !b || !x || !work) return TM_ERR_INVALID;
+  const int nb = tm_pcg_max_blocks(dtype);
+  if (nb <= 0) return TM_ERR_CUDA;
+  if (work_bytes < tm_pcg_workspace_bytes(dtype, n, nb)) return TM_ERR_INDEX;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  char* w = static_cast<char*>(work);
+  if (dtype == TM_F64)
+    return launch_pcg<double>(n, indptr, indices, (const double*)values, (const double*)b, (double*)x, rtol, atol,
+                              maxiter, w, nb, s);
+  if (dtype == TM_F32)
+    return launch_pcg<float>(n, indptr, indices, (const float*)values, (const float*)b, (float*)x, rtol, atol,
+                             maxiter, w, nb, s);
+  return TM_ERR_INVALID;
+}
+
+// Reads the solver record written by the last tm_pcg_jacobi on this
+// workspace (synchronises the stream).
+extern "C" int tm_pcg_result(const void* work, int32_t* iters, double* res, double* bnorm, void* stream) {
+  if (!work) return TM_ERR_INVALID;
+  tmg::PcgState h;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (cudaMemcpyAsync(&h, work, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess) return TM_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return TM_ERR_CUDA;
+  if (iters) *iters = h.iters;
+  if (res) *res = h.res;
+  if (bnorm) *bnorm = h.bnorm;
+  return h.status;
+}
+
+extern "C" int tm_csr_diagonal_inverse(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
+                                       const void* values, void* out, void* stream) {
+  if (n == 0) return TM_OK;
+  if (!indptr || !indices || !values || !out) return TM_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned grid = (unsigned)((n + 255) / 256);
+  if (dtype == TM_F64)
+    tmg::diag_inv_kernel<double><<<grid, 256, 0, s>>>(n, indptr, indices, (const double*)values, (double*)out);
+  else if (dtype == TM_F32)
+    tmg::diag_inv_kernel<float><<<grid, 256, 0, s>>>(n, indptr, indices, (const float*)values, (float*)out);
+  else
+    return TM_ERR_INVALID;
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+extern "C" int tm_gather(int32_t dtype, int64_t n, const int64_t* map, const void* src, void* dst, void* stream) {
+  if (n == 0) return TM_OK;
+  if (!map || !src || !dst) return TM_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned grid = (unsigned)((n + 255) / 256);
+  if (dtype == TM_F64)
+    tmg::gather_kernel<double><<<grid, 256, 0, s>>>(n, map, (const double*)src, (double*)dst);
+  else if (dtype == TM_F32)
+    tmg::gather_kernel<float><<<grid, 256, 0, s>>>(n, map, (const float*)src, (float*)dst);
+  else
+    return TM_ERR_INVALID;
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+extern "C" int tm_scatter(int32_t dtype, int64_t n, const int64_t* map, const void* src, void* dst, void* stream) {
+  if (n == 0) return TM_OK;
+  if (!map || !src || !dst) return TM_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned grid = (unsigned)((n + 255) / 256);
+  if (dtype == TM_F64)
+    tmg::scatter_kernel<double><<<grid, 256, 0, s>>>(n, map, (const double*)src, (double*)dst);
+  else if (dtype == TM_F32)
+    tmg::scatter_kernel<float><<<grid, 256, 0, s>>>(n, map, (const float*)src, (float*)dst);
+  else
+    return TM_ERR_INVALID;
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+extern "C" int tm_condense_rhs(int32_t dtype, int64_t n_inner, const int64_t* inner_dof, const void* rhs,
+                               const int64_t* io_indptr, const int32_t* io_indices, const void* io_values,
+                               const void* u_outer, void* out, void* stream) {
+  if (n_inner == 0) return TM_OK;
+  if (!inner_dof || !rhs || !io_indptr || !out) return TM_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned grid = (unsigned)((n_inner + 255) / 256);
+  if (dtype == TM_F64)
+    tmg::condense_rhs_kernel<double><<<grid, 256, 0, s>>>(n_inner, inner_dof, (const double*)rhs, io_indptr,
+                                                          io_indices, (const double*)io_values,
+                                                          (const double*)u_outer, (double*)out);
+  else if (dtype == TM_F32)
+    tmg::condense_rhs_kernel<float><<<grid, 256, 0, s>>>(n_inner, inner_dof, (const float*)rhs, io_indptr,
+                                                         io_indices, (const float*)io_values,
+                                                         (const float*)u_outer, (float*)out);
+  else
+    return TM_ERR_INVALID;
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}

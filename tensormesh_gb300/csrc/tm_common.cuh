@@ -1,0 +1,121 @@
+// Shared device helpers for the tensormesh_gb300 kernels (sm_103a).
+//
+// df64: an unevaluated sum hi + lo of two floats (~48-bit significand).
+// GB300 executes native FP64 FMA at ~1/73 of the FP32 FMA rate (measured
+// 0.50 T DFMA/s vs 36.8 T FFMA/s on this part), so the FP64 entry points do
+// their arithmetic in df64 on the FP32 pipe and convert to/from double only at
+// the boundary.  The algorithms are the classic error-free transformations:
+// Knuth's TwoSum, Dekker's Fast2Sum, and the FMA-based exact product
+// (Ogita, Rump & Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput.
+// 26(6), 2005), with the "sloppy" double-float add/mul/div/sqrt of Hida, Li &
+// Bailey ("Library for double-double and quad-double arithmetic", 2007),
+// transposed to float pairs.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define TM_HD __host__ __device__ __forceinline__
+#define TM_D __device__ __forceinline__
+
+struct df64 {
+  float hi, lo;
+};
+
+TM_D df64 tm_two_sum(float a, float b) {
+  float s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+TM_D df64 tm_fast_two_sum(float a, float b) {  // requires |a| >= |b| (or a == 0)
+  float s = __fadd_rn(a, b);
+  float e = __fsub_rn(b, __fsub_rn(s, a));
+  return {s, e};
+}
+TM_D df64 operator+(df64 a, df64 b) {
+  df64 s = tm_two_sum(a.hi, b.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return tm_fast_two_sum(s.hi, s.lo);
+}
+TM_D df64 operator-(df64 a) { return {-a.hi, -a.lo}; }
+TM_D df64 operator-(df64 a, df64 b) { return a + (-b); }
+TM_D df64 operator*(df64 a, df64 b) {
+  float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return tm_fast_two_sum(p, e);
+}
+TM_D df64 operator/(df64 a, df64 b) {
+  float q1 = __fdiv_rn(a.hi, b.hi);
+  df64 r = a - df64{q1, 0.f} * b;
+  float q2 = __fdiv_rn(r.hi, b.hi);
+  return tm_fast_two_sum(q1, q2);
+}
+TM_D df64& operator+=(df64& a, df64 b) { a = a + b; return a; }
+TM_D df64& operator-=(df64& a, df64 b) { a = a - b; return a; }
+TM_D df64& operator*=(df64& a, df64 b) { a = a * b; return a; }
+TM_D df64 tm_sqrt(df64 a) {
+  if (a.hi <= 0.f) return {0.f, 0.f};
+  float s = __fsqrt_rn(a.hi);
+  // residual a - s*s, exact in its leading part thanks to the FMA
+  float r = __fadd_rn(__fmaf_rn(-s, s, a.hi), a.lo);
+  return tm_fast_two_sum(s, __fdiv_rn(r, __fadd_rn(s, s)));
+}
+TM_D df64 tm_abs(df64 a) { return a.hi < 0.f ? -a : a; }
+TM_D float tm_approx(df64 a) { return a.hi; }
+
+// double <-> df64.  The split costs one FP64 add; it is applied once per
+// gathered coordinate / coefficient, never inside the element algebra.
+TM_D df64 tm_from_double(double x) {
+  float h = __double2float_rn(x);
+  float l = __double2float_rn(x - (double)h);
+  return {h, l};
+}
+TM_D double tm_to_double(df64 a) { return (double)a.hi + (double)a.lo; }
+
+// Uniform scalar interface so kernels can be written once over
+// R in {float, double, df64}.
+template <class R> struct Num;
+template <> struct Num<float> {
+  static TM_D float from_double(double x) { return (float)x; }
+  static TM_D float from_float(float x) { return x; }
+  static TM_D float zero() { return 0.f; }
+  static TM_D float abs(float x) { return fabsf(x); }
+  static TM_D float sqrt(float x) { return sqrtf(x); }
+  static TM_D bool neg(float x) { return x < 0.f; }
+  static TM_D double to_double(float x) { return (double)x; }
+  static TM_D float to_float(float x) { return x; }
+};
+template <> struct Num<double> {
+  static TM_D double from_double(double x) { return x; }
+  static TM_D double from_float(float x) { return (double)x; }
+  static TM_D double zero() { return 0.0; }
+  static TM_D double abs(double x) { return fabs(x); }
+  static TM_D double sqrt(double x) { return ::sqrt(x); }
+  static TM_D bool neg(double x) { return x < 0.0; }
+  static TM_D double to_double(double x) { return x; }
+  static TM_D float to_float(double x) { return (float)x; }
+};
+template <> struct Num<df64> {
+  static TM_D df64 from_double(double x) { return tm_from_double(x); }
+  static TM_D df64 from_float(float x) { return {x, 0.f}; }
+  static TM_D df64 zero() { return {0.f, 0.f}; }
+  static TM_D df64 abs(df64 x) { return tm_abs(x); }
+  static TM_D df64 sqrt(df64 x) { return tm_sqrt(x); }
+  static TM_D bool neg(df64 x) { return x.hi < 0.f; }
+  static TM_D double to_double(df64 x) { return tm_to_double(x); }
+  static TM_D float to_float(df64 x) { return x.hi + x.lo; }
+};
+
+// Load an input value of storage type T into compute type R.
+template <class R, class T> TM_D R tm_load(T v);
+template <> TM_D float tm_load<float, float>(float v) { return v; }
+template <> TM_D double tm_load<double, double>(double v) { return v; }
+template <> TM_D df64 tm_load<df64, double>(double v) { return tm_from_double(v); }
+template <> TM_D float tm_load<float, double>(double v) { return (float)v; }
+
+template <class T, class R> TM_D T tm_store(R v);
+template <> TM_D float tm_store<float, float>(float v) { return v; }
+template <> TM_D double tm_store<double, double>(double v) { return v; }
+template <> TM_D double tm_store<double, df64>(df64 v) { return tm_to_double(v); }

@@ -1,0 +1,236 @@
+"""Mesh-only precomputation for the deterministic patch assembly.
+
+This replaces the reference's ``from_mesh`` pattern build
+(assemble/element_assembler.py:838-875: scipy coo->csr->coo dedup of the
+element (row, col) pairs plus the per-entry slot map ``elem_eids``) with a
+device-side build in torch ops that produces:
+
+* the node-level CSR pattern (indptr, indices) in canonical order -- the
+  same unique, row-major, column-sorted pairs the reference's ``edges`` hold;
+* a partition of the nodes into *patches* by recursive coordinate bisection
+  (RCB); each patch owns a set of CSR rows and lists every element touching
+  them, with a patch-local vertex table and, for each owned row, its
+  incidences (element, local vertex) sorted by element together with the
+  position of every column inside the row.
+
+Everything is computed with torch ops, so it runs on the GPU when the mesh
+lives there (and on the CPU in unit tests).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import torch
+
+from . import _lib
+
+
+@dataclass
+class NodePattern:
+    n_points: int
+    indptr: torch.Tensor    # int64 [N+1]
+    indices: torch.Tensor   # int32 [nnz]
+    slots: torch.Tensor     # int64 [E, B, B] global slot of each element entry
+
+    @property
+    def nnz(self) -> int:
+        return int(self.indices.shape[0])
+
+
+def node_pattern(elements: torch.Tensor, n_points: int) -> NodePattern:
+    """Unique element (row, col) pairs in canonical CSR order
+    (element_assembler.py:838-866)."""
+    E, B = elements.shape
+    el = elements.long()
+    u = el.unsqueeze(2).expand(E, B, B).reshape(-1)
+    v = el.unsqueeze(1).expand(E, B, B).reshape(-1)
+    key = u * n_points + v
+    uniq, inv = torch.unique(key, sorted=True, return_inverse=True)
+    rows = torch.div(uniq, n_points, rounding_mode="floor")
+    cols = uniq - rows * n_points
+    counts = torch.bincount(rows, minlength=n_points)
+    indptr = torch.zeros(n_points + 1, dtype=torch.int64, device=elements.device)
+    indptr[1:] = torch.cumsum(counts, 0)
+    return NodePattern(n_points, indptr, cols.to(torch.int32), inv.view(E, B, B))
+
+
+def block_pattern(indptr: torch.Tensor, indices: torch.Tensor, H: int):
+    """Dof-level canonical CSR of the H x H block expansion
+    row = H*i + a, col = H*j + b (sparse/matrix.py:355-375 followed by the
+    canonical sort).  Row (H*i + a) lists cols H*j + b for j in row i,
+    b in 0..H-1."""
+    if H == 1:
+        return indptr, indices
+    n = indptr.shape[0] - 1
+    deg = indptr[1:] - indptr[:-1]
+    dof_deg = (deg * H).repeat_interleave(H)
+    dptr = torch.zeros(n * H + 1, dtype=torch.int64, device=indptr.device)
+    dptr[1:] = torch.cumsum(dof_deg, 0)
+    # node row i -> H copies of [H*c + b for c in cols(i) for b]
+    blk = (indices.long().unsqueeze(1) * H + torch.arange(H, device=indptr.device)).reshape(-1)  # [nnz*H]
+    # for each node row, repeat its block row H times
+    node_of_slot = torch.repeat_interleave(torch.arange(n, device=indptr.device), deg)
+    start_blk = indptr[:-1] * H
+    out = torch.empty(int(dptr[-1]), dtype=torch.int32, device=indptr.device)
+    # dof row (i, a) occupies out[dptr[i*H+a] : +deg_i*H] = blk[start_blk[i] : start_blk[i] + deg_i*H]
+    pos_in_row = torch.arange(blk.shape[0], device=indptr.device) - start_blk[node_of_slot.repeat_interleave(H)]
+    node_blk = node_of_slot.repeat_interleave(H)
+    for a in range(H):
+        dst = dptr[node_blk * H + a] + pos_in_row
+        out[dst] = blk.to(torch.int32)
+    return dptr, out
+
+
+def rcb_partition(coords: torch.Tensor, n_levels: int) -> torch.Tensor:
+    """Recursive coordinate bisection: split every segment at its median
+    along its longest extent, ``n_levels`` times.  Returns the part id of
+    each point (parts numbered in RCB leaf order, spatially coherent)."""
+    N = coords.shape[0]
+    dev = coords.device
+    c = coords.to(torch.float64)
+    D = c.shape[1]
+    perm = torch.arange(N, device=dev)
+    seg = torch.zeros(N, dtype=torch.int64, device=dev)
+    ar = torch.arange(N, device=dev)
+    for level in range(n_levels):
+        nseg = 1 << level
+        cp = c[perm]
+        idx = seg.unsqueeze(1).expand(N, D)
+        mx = torch.full((nseg, D), -math.inf, dtype=torch.float64, device=dev).scatter_reduce(0, idx, cp, "amax")
+        mn = torch.full((nseg, D), math.inf, dtype=torch.float64, device=dev).scatter_reduce(0, idx, cp, "amin")
+        axis = torch.argmax(mx - mn, dim=1)
+        val = cp[ar, axis[seg]]
+        o1 = torch.argsort(val, stable=True)
+        o2 = torch.argsort(seg[o1], stable=True)
+        order = o1[o2]
+        perm = perm[order]
+        seg = seg[order]
+        counts = torch.bincount(seg, minlength=nseg)
+        start = torch.cumsum(counts, 0) - counts
+        pos = ar - start[seg]
+        seg = 2 * seg + (pos >= (counts[seg] + 1) // 2).long()
+    part = torch.empty(N, dtype=torch.int64, device=dev)
+    part[perm] = seg
+    return part
+
+
+class PatchPlan:
+    """Device arrays of the patch structure plus the ctypes view of them."""
+
+    def __init__(self, elements: torch.Tensor, coords: torch.Tensor, pattern: NodePattern,
+                 slot_budget: int = 6144, max_rows_cap: int = 2048):
+        dev = elements.device
+        E, B = elements.shape
+        N = pattern.n_points
+        self.n_elements, self.n_basis, self.n_points = E, B, N
+        el = elements.long()
+        indptr = pattern.indptr
+        deg = indptr[1:] - indptr[:-1]
+        if E > 0 and int(deg.max()) > 255:
+            raise NotImplementedError("a CSR row longer than 255 entries is not supported by the patch plan")
+
+        # -- partition: enough RCB levels that every patch fits the slot budget
+        avg_deg = float(deg.float().mean()) if N else 1.0
+        target_rows = max(16, min(max_rows_cap, int(slot_budget / max(avg_deg, 1.0))))
+        n_levels = max(0, math.ceil(math.log2(max(1, N) / target_rows)))
+        while True:
+            part = rcb_partition(coords, n_levels) if N else torch.zeros(0, dtype=torch.int64, device=dev)
+            n_parts = 1 << n_levels
+            slots_per_part = torch.zeros(n_parts, dtype=torch.int64, device=dev).index_add_(0, part, deg)
+            rows_per_part = torch.bincount(part, minlength=n_parts)
+            if N == 0 or (int(slots_per_part.max()) <= 2 * slot_budget and int(rows_per_part.max()) <= max_rows_cap):
+                break
+            n_levels += 1
+        self.n_patches = n_parts
+
+        # -- owned rows, sorted by (patch, node id)
+        row_order = torch.argsort(part * N + torch.arange(N, device=dev))
+        rows = row_order
+        rptr = torch.zeros(n_parts + 1, dtype=torch.int64, device=dev)
+        rptr[1:] = torch.cumsum(rows_per_part, 0)
+        row_deg = deg[rows]
+        cum = torch.zeros(N + 1, dtype=torch.int64, device=dev)
+        cum[1:] = torch.cumsum(row_deg, 0)                             # global exclusive prefix
+        racc = cum[:-1] - cum[rptr[:-1]].repeat_interleave(rows_per_part)  # patch-relative
+        row_rank = torch.empty(N, dtype=torch.int64, device=dev)
+        row_rank[rows] = torch.arange(N, device=dev)
+
+        # -- (patch, element) pairs: elements touching each patch
+        pe_key = (part[el] * E + torch.arange(E, device=dev).unsqueeze(1)).reshape(-1)
+        pairs = torch.unique(pe_key, sorted=True)
+        pair_patch = torch.div(pairs, E, rounding_mode="floor")
+        pair_elem = pairs - pair_patch * E
+        elems_per_part = torch.bincount(pair_patch, minlength=n_parts)
+        eptr = torch.zeros(n_parts + 1, dtype=torch.int64, device=dev)
+        eptr[1:] = torch.cumsum(elems_per_part, 0)
+        if E and int(elems_per_part.max()) > 65535:
+            raise NotImplementedError("patch with more than 65535 elements")
+
+        # -- patch-local vertex tables
+        pconn = el[pair_elem]                                           # [n_pairs, B]
+        pv_key = pair_patch.unsqueeze(1) * N + pconn
+        vkeys = torch.unique(pv_key.reshape(-1), sorted=True)
+        vtx_patch = torch.div(vkeys, N, rounding_mode="floor")
+        vtx = vkeys - vtx_patch * N
+        verts_per_part = torch.bincount(vtx_patch, minlength=n_parts)
+        vptr = torch.zeros(n_parts + 1, dtype=torch.int64, device=dev)
+        vptr[1:] = torch.cumsum(verts_per_part, 0)
+        if E and int(verts_per_part.max()) > 65535:
+            raise NotImplementedError("patch with more than 65535 vertices")
+        local = torch.searchsorted(vkeys, pv_key) - vptr[pair_patch].unsqueeze(1)
+
+        # -- incidences of owned rows
+        owned = part[pconn] == pair_patch.unsqueeze(1)                 # [n_pairs, B]
+        pi, a = torch.nonzero(owned, as_tuple=True)
+        inc_row = pconn[pi, a]
+        inc_local_elem = pi - eptr[pair_patch[pi]]
+        order = torch.argsort(row_rank[inc_row] * (1 << 20) + inc_local_elem)
+        pi, a, inc_row, inc_local_elem = pi[order], a[order], inc_row[order], inc_local_elem[order]
+        ge = pair_elem[pi]
+        inc_pos = pattern.slots[ge, a, :] - indptr[inc_row].unsqueeze(1)  # [n_inc, B]
+        inc_per_row = torch.bincount(row_rank[inc_row], minlength=N)
+        iptr = torch.zeros(N + 1, dtype=torch.int64, device=dev)
+        iptr[1:] = torch.cumsum(inc_per_row, 0)
+
+        i32 = torch.int32
+        self.vptr = vptr.to(i32)
+        self.vtx = vtx.to(i32)
+        self.eptr = eptr.to(i32)
+        self.elem = pair_elem.to(i32)
+        self.econn = local.to(i32).to(torch.int16).contiguous()        # uint16 bit pattern
+        self.rptr = rptr.to(i32)
+        self.rows = rows.to(i32)
+        self.racc = racc.to(i32)
+        self.iptr = iptr.to(i32)
+        self.inc_elem = inc_local_elem.to(i32).to(torch.int16).contiguous()
+        self.inc_a = a.to(torch.uint8).contiguous()
+        self.inc_pos = inc_pos.to(torch.uint8).contiguous()
+        self.indptr = indptr.contiguous()
+        self.max_vtx = int(verts_per_part.max()) if E else 0
+        self.max_slots = int(slots_per_part.max()) if N else 0
+        self.max_rows = int(rows_per_part.max()) if N else 0
+        self.max_elems = int(elems_per_part.max()) if E else 0
+        self.n_pairs = int(pairs.shape[0])
+        self.n_incidences = int(pi.shape[0])
+        if int(iptr[-1]) >= 2**31 or self.n_pairs * B >= 2**31:
+            raise NotImplementedError("mesh too large for 32-bit plan offsets")
+
+    @property
+    def redundancy(self) -> float:
+        """Element computations per element (patch halo overhead)."""
+        return self.n_pairs / max(1, self.n_elements)
+
+    def to_struct(self) -> _lib.PatchPlan:
+        s = _lib.PatchPlan()
+        s.n_patches, s.n_elements, s.n_points, s.n_basis = self.n_patches, self.n_elements, self.n_points, self.n_basis
+        for name in ("vptr", "vtx", "eptr", "elem", "econn", "rptr", "rows", "racc", "iptr",
+                     "inc_elem", "inc_a", "inc_pos", "indptr"):
+            setattr(s, name, getattr(self, name).data_ptr())
+        s.max_vtx, s.max_slots, s.max_rows, s.max_elems = self.max_vtx, self.max_slots, self.max_rows, self.max_elems
+        return s
+
+    def nbytes(self) -> int:
+        return sum(getattr(self, n).numel() * getattr(self, n).element_size()
+                   for n in ("vptr", "vtx", "eptr", "elem", "econn", "rptr", "rows", "racc", "iptr",
+                             "inc_elem", "inc_a", "inc_pos"))

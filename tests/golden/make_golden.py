@@ -1,0 +1,252 @@
+"""Generate the golden fixtures in this folder by running the reference
+TensorMesh package itself (CPU, float64).
+
+Run from the repository root with the reference source tree on the machine:
+
+    python tests/golden/make_golden.py /path/to/TensorMesh
+
+The reference needs two packages that are not installed here (``meshio`` and
+``torch_sla``); ``tests/golden/_stubs`` provides the minimal containers the
+reference touches on this path (no numerics).  The fixtures written are small
+``.npz`` files: every array in them is an input this script built or an
+output of the reference's own ``ElementAssembler`` / ``NodeAssembler`` /
+``Condenser`` / ``SparseSolveScipy`` calls.  Tests read only the ``.npz``
+files, never the reference.
+"""
+from __future__ import annotations
+
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def square_mesh(n, jitter=0.0, seed=0):
+    """Unit square, n x n cells, nodes x-fastest, cell (i,j) with corners
+    a=(i,j) b=(i+1,j) c=(i+1,j+1) d=(i,j+1) split into (a,b,c), (a,c,d)."""
+    xs = np.linspace(0.0, 1.0, n + 1)
+    X, Y = np.meshgrid(xs, xs, indexing="xy")
+    pts = np.stack([X.ravel(), Y.ravel()], 1)
+    bd = (np.isclose(pts[:, 0], 0) | np.isclose(pts[:, 0], 1) | np.isclose(pts[:, 1], 0) | np.isclose(pts[:, 1], 1))
+    if jitter:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-jitter, jitter, pts.shape) / n
+        d[bd] = 0.0
+        pts = pts + d
+    idx = lambda i, j: j * (n + 1) + i  # noqa: E731
+    tris = []
+    for j in range(n):
+        for i in range(n):
+            a, b, c, d_ = idx(i, j), idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)
+            tris += [(a, b, c), (a, c, d_)]
+    return pts, np.array(tris, dtype=np.int64), bd
+
+
+_KUHN = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+
+
+def cube_mesh(n, jitter=0.0, seed=0):
+    """Unit cube, n^3 cells, nodes x-fastest then y then z; each cell split
+    into the 6 Kuhn tetrahedra sharing the diagonal v000 -> v111, one per
+    axis permutation in lexicographic order."""
+    xs = np.linspace(0.0, 1.0, n + 1)
+    Z, Y, X = np.meshgrid(xs, xs, xs, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+    bd = np.zeros(len(pts), dtype=bool)
+    for k in range(3):
+        bd |= np.isclose(pts[:, k], 0) | np.isclose(pts[:, k], 1)
+    if jitter:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-jitter, jitter, pts.shape) / n
+        d[bd] = 0.0
+        pts = pts + d
+    idx = lambda i, j, k: (k * (n + 1) + j) * (n + 1) + i  # noqa: E731
+    tets = []
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                for perm in _KUHN:
+                    v = [i, j, k]
+                    path = [idx(*v)]
+                    for ax in perm:
+                        v[ax] += 1
+                        path.append(idx(*v))
+                    tets.append(tuple(path))
+    return pts, np.array(tets, dtype=np.int64), bd
+
+
+_TRI_EDGES = [(1, 2), (0, 2), (0, 1)]
+_TET_EDGES = [(2, 3), (1, 3), (1, 2), (0, 3), (0, 2), (0, 1)]
+
+
+def to_p2(pts, cells, bd):
+    """Insert edge midpoints: unique edges sorted by (min, max) are numbered
+    after the vertices; each element lists its midpoints in the reference
+    element's edge order."""
+    dim = pts.shape[1]
+    loc = _TRI_EDGES if dim == 2 else _TET_EDGES
+    pairs = np.stack([np.sort(cells[:, [a, b]], axis=1) for a, b in loc], 1)  # [E, ne, 2]
+    flat = pairs.reshape(-1, 2)
+    key = flat[:, 0] * len(pts) + flat[:, 1]
+    uniq, inv = np.unique(key, return_inverse=True)
+    u0, u1 = uniq // len(pts), uniq % len(pts)
+    mid = 0.5 * (pts[u0] + pts[u1])
+    new_pts = np.concatenate([pts, mid], 0)
+    new_cells = np.concatenate([cells, len(pts) + inv.reshape(cells.shape[0], len(loc))], 1)
+    new_bd = np.concatenate([bd, bd[u0] & bd[u1]])
+    return new_pts, new_cells, new_bd
+
+
+def main(ref_root):
+    sys.path.insert(0, os.path.join(HERE, "_stubs"))
+    sys.path.insert(0, ref_root)
+    import torch
+    import meshio
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    import tensormesh as tm
+    from tensormesh.functional.elasticity import voigt_shape_grad, voigt_stiffness
+    from tensormesh.sparse.solve.scipy_solve import SparseSolveScipy
+
+    torch.set_num_threads(max(1, os.cpu_count() or 1))
+
+    def mk_mesh(pts, cells, bd, etype):
+        p3 = pts if pts.shape[1] == 3 else np.concatenate([pts, np.zeros((len(pts), 1))], 1)
+        m = meshio.Mesh(p3, [(etype, cells)], point_data={"is_boundary": bd})
+        return tm.Mesh(m)
+
+    def canon(Kmat):
+        c = Kmat.to_scipy_coo().tocsr()
+        c.sum_duplicates()
+        c.sort_indices()
+        return c.indptr.astype(np.int64), c.indices.astype(np.int64), c.data.astype(np.float64)
+
+    class KappaLaplace(tm.ElementAssembler):
+        def forward(self, gradu, gradv, kappa):
+            return kappa * (gradu @ gradv)
+
+    class KappaMass(tm.ElementAssembler):
+        def forward(self, u, v, kappa):
+            return kappa * u * v
+
+    NU = 0.3
+
+    class EElasticity(tm.ElementAssembler):
+        def forward(self, gradu, gradv, E):
+            Ba = voigt_shape_grad(gradu)
+            Bb = voigt_shape_grad(gradv)
+            C = voigt_stiffness(1.0, NU, gradu.shape[0]).to(dtype=gradu.dtype)
+            return E * (Ba.T @ C @ Bb)
+
+    out = {}
+    # ------------------------------------------------------------------ forms
+    meshes = {
+        "triangle": square_mesh(4, jitter=0.25, seed=1),
+        "tetra": cube_mesh(2, jitter=0.2, seed=2),
+    }
+    meshes["triangle6"] = to_p2(*meshes["triangle"])
+    meshes["tetra10"] = to_p2(*meshes["tetra"])
+    rng = np.random.default_rng(7)
+    for etype, (pts, cells, bd) in meshes.items():
+        mesh = mk_mesh(pts, cells, bd, etype)
+        n_el = cells.shape[0]
+        coef = np.exp(rng.normal(size=n_el))
+        out[f"{etype}/points"] = pts
+        out[f"{etype}/elements"] = cells
+        out[f"{etype}/boundary"] = bd
+        out[f"{etype}/coef"] = coef
+        for q in (1, 2, 3):
+            cases = {
+                "laplace": lambda: tm.LaplaceElementAssembler.from_mesh(mesh, quadrature_order=q)(mesh.points),
+                "mass": lambda: tm.MassElementAssembler.from_mesh(mesh, quadrature_order=q)(mesh.points),
+                "elasticity": lambda: tm.LinearElasticityElementAssembler.from_mesh(
+                    mesh, quadrature_order=q, E=2.5, nu=NU)(mesh.points),
+                "laplace_kappa": lambda: KappaLaplace.from_mesh(mesh, quadrature_order=q)(
+                    mesh.points, element_data={"kappa": torch.from_numpy(coef)}),
+                "mass_kappa": lambda: KappaMass.from_mesh(mesh, quadrature_order=q)(
+                    mesh.points, element_data={"kappa": torch.from_numpy(coef)}),
+                "elasticity_E": lambda: EElasticity.from_mesh(mesh, quadrature_order=q)(
+                    mesh.points, element_data={"E": torch.from_numpy(coef)}),
+            }
+            for name, fn in cases.items():
+                K = fn()
+                ip, ix, dv = canon(K)
+                out[f"{etype}/{name}/q{q}/indptr"] = ip
+                out[f"{etype}/{name}/q{q}/indices"] = ix
+                out[f"{etype}/{name}/q{q}/data"] = dv
+            # loads
+            f_nodes = np.sin(3.0 * pts[:, 0]) + pts[:, 1] ** 2
+            loads = {
+                "const": lambda: tm.const_node_assembler(1.0).from_mesh(mesh, quadrature_order=q)(mesh.points),
+                "func": lambda: tm.func_node_assembler(
+                    lambda x: 2 * math.pi ** 2 * torch.sin(math.pi * x[..., 0]) * torch.sin(math.pi * x[..., 1])
+                ).from_mesh(mesh, quadrature_order=q)(mesh.points),
+                "point": lambda: PointLoad.from_mesh(mesh, quadrature_order=q)(
+                    mesh.points, point_data={"f": torch.from_numpy(f_nodes)}),
+                "vector": lambda: tm.const_node_assembler(
+                    torch.tensor([0.5, -1.0] if pts.shape[1] == 2 else [0.0, 0.3, -1.0], dtype=torch.float64)
+                ).from_mesh(mesh, quadrature_order=q)(mesh.points),
+            }
+
+            class PointLoad(tm.NodeAssembler):
+                def forward(self, v, f):
+                    return v * f
+
+            for name, fn in loads.items():
+                out[f"{etype}/load_{name}/q{q}"] = fn().detach().numpy().astype(np.float64)
+            out[f"{etype}/f_nodes"] = f_nodes
+        # the reference's own (unsorted) edges for the scalar pattern claim
+        asm = tm.LaplaceElementAssembler.from_mesh(mesh, quadrature_order=1)
+        out[f"{etype}/ref_edges"] = asm.edges.numpy().astype(np.int64)
+
+    # -------------------------------------------------- C1 Poisson, 64 x 64
+    pts, cells, bd = square_mesh(64)
+    mesh = mk_mesh(pts, cells, bd, "triangle")
+    K = tm.LaplaceElementAssembler.from_mesh(mesh, quadrature_order=1)(mesh.points)
+    fsrc = tm.func_node_assembler(
+        lambda x: 2 * math.pi ** 2 * torch.sin(math.pi * x[..., 0]) * torch.sin(math.pi * x[..., 1]))
+    b = fsrc.from_mesh(mesh, quadrature_order=1)(mesh.points)
+    cond = tm.Condenser(mesh.boundary_mask)
+    K_ii, f_i = cond(K, b)
+    ip, ix, dv = canon(K)
+    c = K_ii.to_scipy_coo().tocsr()
+    c.sum_duplicates(); c.sort_indices()
+    u_i = spla.spsolve(c.tocsc(), f_i.numpy())
+    u = cond.recover(torch.from_numpy(u_i)).numpy()
+    out.update({
+        "c1/points": pts, "c1/elements": cells, "c1/boundary": bd,
+        "c1/K_indptr": ip, "c1/K_indices": ix, "c1/K_data": dv, "c1/b": b.numpy(),
+        "c1/Kii_indptr": c.indptr.astype(np.int64), "c1/Kii_indices": c.indices.astype(np.int64),
+        "c1/Kii_data": c.data, "c1/f_i": f_i.numpy(), "c1/u": u,
+    })
+
+    # --------------------------------------------- adjoint (compliance), 12^2
+    pts, cells, bd = square_mesh(12, jitter=0.2, seed=3)
+    mesh = mk_mesh(pts, cells, bd, "triangle")
+    g = np.random.default_rng(11).normal(size=cells.shape[0])
+    kappa = torch.tensor(np.exp(g), requires_grad=True)
+    x = torch.tensor(pts, requires_grad=True)
+    Kasm = KappaLaplace.from_mesh(mesh, quadrature_order=1)
+    Basm = tm.const_node_assembler(1.0).from_mesh(mesh, quadrature_order=1)
+    K = Kasm(x, element_data={"kappa": kappa})
+    bvec = Basm(x)
+    cond = tm.Condenser(mesh.boundary_mask)
+    K_ii, f_i = cond(K, bvec)
+    u_i = SparseSolveScipy.apply(K_ii.values, K_ii.row, K_ii.col, K_ii.shape, f_i)
+    u = cond.recover(u_i)
+    J = (bvec * u).sum()
+    J.backward()
+    out.update({
+        "adj/points": pts, "adj/elements": cells, "adj/boundary": bd, "adj/kappa": np.exp(g),
+        "adj/J": np.array(J.item()), "adj/dJ_dkappa": kappa.grad.numpy(), "adj/dJ_dx": x.grad.numpy(),
+        "adj/u": u.detach().numpy(),
+    })
+    np.savez_compressed(os.path.join(HERE, "reference_fem.npz"), **out)
+    print("wrote", len(out), "arrays")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

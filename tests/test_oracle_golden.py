@@ -1,0 +1,95 @@
+"""Pin the CPU oracle to fixtures produced by the reference package itself
+(tests/golden/make_golden.py): same CSR pattern, values within 1e-12
+relative (max-norm over nnz, relative to max|K|)."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import fem
+
+ETYPES = ["triangle", "triangle6", "tetra", "tetra10"]
+CASES = ["laplace", "mass", "elasticity", "laplace_kappa", "mass_kappa", "elasticity_E"]
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("etype", ETYPES)
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("q", [1, 2, 3])
+def test_oracle_matches_reference_assembly(golden, etype, case, q):
+    pts = golden[f"{etype}/points"]
+    el = golden[f"{etype}/elements"]
+    coef = golden[f"{etype}/coef"]
+    form = case.split("_")[0]
+    c = None
+    if case == "elasticity":
+        c = 2.5
+    elif case != form:
+        c = coef
+    ip, ix, dv = fem.assemble_csr(pts, el, etype, form, q, coef=c, nu=0.3)
+    key = f"{etype}/{case}/q{q}"
+    np.testing.assert_array_equal(ip, golden[key + "/indptr"])
+    np.testing.assert_array_equal(ix, golden[key + "/indices"])
+    assert rel_err(dv, golden[key + "/data"]) <= 1e-12
+
+
+@pytest.mark.parametrize("etype", ETYPES)
+@pytest.mark.parametrize("q", [1, 2, 3])
+def test_oracle_matches_reference_loads(golden, etype, q):
+    pts = golden[f"{etype}/points"]
+    el = golden[f"{etype}/elements"]
+    dim = pts.shape[1]
+    f = lambda x: 2 * math.pi ** 2 * np.sin(math.pi * x[..., 0]) * np.sin(math.pi * x[..., 1])  # noqa: E731
+    got = {
+        "const": fem.assemble_load(pts, el, etype, q, "const", 1.0),
+        "func": fem.assemble_load(pts, el, etype, q, "func", f),
+        "point": fem.assemble_load(pts, el, etype, q, "point", golden[f"{etype}/f_nodes"]),
+        "vector": fem.assemble_load(pts, el, etype, q, "const", [0.5, -1.0] if dim == 2 else [0.0, 0.3, -1.0]),
+    }
+    for name, v in got.items():
+        ref = golden[f"{etype}/load_{name}/q{q}"]
+        assert v.shape == ref.shape, name
+        assert rel_err(v, ref) <= 1e-12, name
+
+
+def test_scalar_pattern_is_reference_edge_order(golden):
+    """The reference's scalar ``edges`` are already canonical CSR order
+    (element_assembler.py:851-856): row-major, sorted columns."""
+    for etype in ETYPES:
+        e = golden[f"{etype}/ref_edges"]
+        ip, ix, _ = fem.node_pattern(golden[f"{etype}/elements"], golden[f"{etype}/points"].shape[0])
+        rows = np.repeat(np.arange(ip.shape[0] - 1), np.diff(ip))
+        np.testing.assert_array_equal(e[0], rows)
+        np.testing.assert_array_equal(e[1], ix)
+
+
+def test_oracle_c1_poisson_pipeline(golden):
+    pts, el, bd = golden["c1/points"], golden["c1/elements"], golden["c1/boundary"]
+    ip, ix, dv = fem.assemble_csr(pts, el, "triangle", "laplace", 1)
+    np.testing.assert_array_equal(ip, golden["c1/K_indptr"])
+    np.testing.assert_array_equal(ix, golden["c1/K_indices"])
+    assert rel_err(dv, golden["c1/K_data"]) <= 1e-12
+    f = lambda x: 2 * math.pi ** 2 * np.sin(math.pi * x[..., 0]) * np.sin(math.pi * x[..., 1])  # noqa: E731
+    b = fem.assemble_load(pts, el, "triangle", 1, "func", f)
+    assert rel_err(b, golden["c1/b"]) <= 1e-12
+    iptr, iind, ival, fi = fem.condense(ip, ix, dv, bd, None, b)
+    np.testing.assert_array_equal(iptr, golden["c1/Kii_indptr"])
+    np.testing.assert_array_equal(iind, golden["c1/Kii_indices"])
+    assert rel_err(ival, golden["c1/Kii_data"]) <= 1e-12
+    assert rel_err(fi, golden["c1/f_i"]) <= 1e-12
+    u = fem.recover(fem.spsolve(iptr, iind, ival, fi), bd)
+    assert rel_err(u, golden["c1/u"]) <= 1e-10
+    # PCG reaches the same solution
+    x, it, res = fem.pcg_jacobi(iptr, iind, ival, fi, rtol=1e-12)
+    assert res <= 1e-11
+    assert rel_err(fem.recover(x, bd), golden["c1/u"]) <= 1e-9
+
+
+def test_oracle_adjoint_kappa_matches_reference_autograd(golden):
+    pts, el, bd, kappa = golden["adj/points"], golden["adj/elements"], golden["adj/boundary"], golden["adj/kappa"]
+    u = golden["adj/u"]
+    g = fem.compliance_gradients_kappa(pts, el, "triangle", 1, kappa, u)
+    assert rel_err(g, golden["adj/dJ_dkappa"]) <= 1e-10

@@ -1,0 +1,108 @@
+"""Host-side logic on the CPU: structured meshes, the canonical pattern, the
+block expansion and the patch plan.  The patch plan is checked by replaying
+the kernel's gather order (phase B of the assembly kernel) in numpy with the
+oracle's element matrices: it must reproduce the oracle CSR exactly in
+pattern and to rounding in values."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import fem
+from tensormesh_gb300 import Mesh
+from tensormesh_gb300.plan import PatchPlan, block_pattern, node_pattern
+
+
+def _meshes():
+    sq = Mesh.gen_unit_square(5)
+    cu = Mesh.gen_unit_cube(3)
+    return {"triangle": sq, "triangle6": sq.to_p2(), "tetra": cu, "tetra10": cu.to_p2()}
+
+
+def test_structured_meshes_match_fixture_numbering(golden):
+    """The generators reproduce the numbering of the golden meshes (built by
+    the fixture script with its own code)."""
+    c1 = Mesh.gen_unit_square(64)
+    np.testing.assert_array_equal(c1.cells["triangle"].numpy(), golden["c1/elements"])
+    np.testing.assert_allclose(c1.points.numpy(), golden["c1/points"], rtol=0, atol=0)
+    np.testing.assert_array_equal(c1.boundary_mask.numpy(), golden["c1/boundary"])
+
+
+def test_kuhn_cube_counts():
+    m = Mesh.gen_unit_cube(4)
+    assert m.cells["tetra"].shape == (6 * 64, 4)
+    p = node_pattern(m.cells["tetra"], m.n_points)
+    n = 4
+    assert p.nnz == (n + 1) ** 3 + 2 * (3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1) + n ** 3)
+    # every Kuhn tet has the same volume 1/(6 n^3) and covers the cube
+    X = m.points[m.cells["tetra"]].double()
+    vol = torch.det(X[:, 1:] - X[:, :1]).abs() / 6
+    assert torch.allclose(vol, torch.full_like(vol, 1 / (6 * n ** 3)))
+
+
+@pytest.mark.parametrize("etype", ["triangle", "triangle6", "tetra", "tetra10"])
+def test_pattern_matches_oracle(etype):
+    m = _meshes()[etype]
+    el = m.cells[etype]
+    p = node_pattern(el, m.n_points)
+    ip, ix, slots = fem.node_pattern(el.numpy(), m.n_points)
+    np.testing.assert_array_equal(p.indptr.numpy(), ip)
+    np.testing.assert_array_equal(p.indices.numpy(), ix)
+    np.testing.assert_array_equal(p.slots.numpy(), slots)
+    for H in (2, 3):
+        dp, di = block_pattern(p.indptr, p.indices, H)
+        op, oi = fem.block_pattern(ip, ix, H)
+        np.testing.assert_array_equal(dp.numpy(), op)
+        np.testing.assert_array_equal(di.numpy(), oi)
+
+
+def replay_plan(plan: PatchPlan, Ke: np.ndarray, nnz: int) -> np.ndarray:
+    """numpy replay of the kernel's phase B + write-out for scalar forms."""
+    out = np.full(nnz, np.nan)
+    B = plan.n_basis
+    rptr, rows, racc = plan.rptr.numpy(), plan.rows.numpy(), plan.racc.numpy()
+    eptr, elem = plan.eptr.numpy(), plan.elem.numpy()
+    iptr = plan.iptr.numpy()
+    inc_elem = plan.inc_elem.numpy().astype(np.int64) & 0xFFFF
+    inc_a = plan.inc_a.numpy()
+    inc_pos = plan.inc_pos.numpy().reshape(-1, B)
+    indptr = plan.indptr.numpy()
+    for p in range(plan.n_patches):
+        for lr in range(rptr[p], rptr[p + 1]):
+            r = rows[lr]
+            deg = indptr[r + 1] - indptr[r]
+            acc = np.zeros(deg)
+            prev = -1
+            for k in range(iptr[lr], iptr[lr + 1]):
+                le = inc_elem[k]
+                assert le > prev  # sorted by element, as phase B requires
+                prev = le
+                e = elem[eptr[p] + le]
+                a = inc_a[k]
+                for b in range(B):
+                    acc[inc_pos[k, b]] += Ke[e, a, b]
+            out[indptr[r]:indptr[r + 1]] = acc
+    return out
+
+
+@pytest.mark.parametrize("etype", ["triangle", "triangle6", "tetra", "tetra10"])
+@pytest.mark.parametrize("budget", [64, 300, 100000])
+def test_patch_plan_replay_reproduces_oracle(etype, budget):
+    m = _meshes()[etype]
+    el = m.cells[etype]
+    pts = m.points.numpy()
+    p = node_pattern(el, m.n_points)
+    plan = PatchPlan(el, m.points, p, slot_budget=budget)
+    assert plan.n_incidences == el.shape[0] * el.shape[1]
+    # every row owned exactly once
+    assert sorted(plan.rows.tolist()) == list(range(m.n_points))
+    # local connectivity round-trips to the global one
+    econn = plan.econn.numpy().astype(np.int64) & 0xFFFF
+    vptr, vtx, eptr = plan.vptr.numpy(), plan.vtx.numpy(), plan.eptr.numpy()
+    for pp in range(plan.n_patches):
+        for le in range(eptr[pp], eptr[pp + 1]):
+            e = plan.elem[le].item()
+            np.testing.assert_array_equal(vtx[vptr[pp] + econn[le]], el[e].numpy())
+    Ke = fem.element_matrices(pts, el.numpy(), etype, "laplace", 2)
+    ip, ix, dv = fem.assemble_csr(pts, el.numpy(), etype, "laplace", 2)
+    got = replay_plan(plan, Ke, ix.shape[0])
+    assert np.max(np.abs(got - dv)) <= 1e-13 * np.max(np.abs(dv))
