@@ -160,6 +160,53 @@ int tm_segment_sum(int32_t dtype, int64_t n_segments, const int64_t* ptr, const 
                    const void* src, void* dst, void* stream);
 
 /*
+ * Batched assemble + Jacobi-PCG of many independent meshes in ONE persistent
+ * launch (capturable in a CUDA graph).  The union mesh's patch plan must keep
+ * each instance's patches contiguous (inst_pbeg) and its rows contiguous
+ * (inst_rbeg).  Clusters of `cluster` CTAs pop instances in `order` and, per
+ * instance, assemble K (mat, float32) and b (load, float32) into mat->out /
+ * load->out, then run Jacobi-PCG on the non-Dirichlet dofs to
+ * ||r|| <= rtol ||b||, writing x and per-instance status / iterations /
+ * residual.  work: 6 * n_rows floats.  queue: one device uint.
+ * Replaces the reference's per-mesh Python loop of assembler calls and
+ * solves (no batched path exists in the reference).
+ */
+typedef struct tm_batched_args {
+  int32_t element;     /* TM_TRI3 or TM_TET4 */
+  int32_t cluster;     /* CTAs per cluster (1..16) */
+  int32_t n_clusters;  /* persistent clusters launched */
+  int32_t n_inst;
+  int32_t maxiter;
+  int32_t chunk;       /* staging chunk of the patch assembly */
+  float rtol;
+  int32_t pad0;
+  int64_t n_rows;      /* rows of the union */
+  int64_t smem_bytes;  /* dynamic shared memory per CTA */
+  const tm_patch_plan* plan;
+  const tm_assemble_args* mat;
+  const tm_assemble_args* load;
+  const int32_t* order;
+  const int32_t* inst_pbeg;
+  const int64_t* inst_rbeg;
+  const int32_t* indices;   /* node-level CSR column indices of the union */
+  const uint8_t* dirichlet; /* [n_rows] */
+  float* x;
+  void* work;
+  int32_t* status;
+  int32_t* iters;
+  float* resid;
+  unsigned int* queue;
+  void* stream;
+} tm_batched_args;
+
+int tm_batched_assemble_pcg(const tm_batched_args* args, void* stream);
+/* clusters of the given size that fit on the device at once (occupancy) */
+int tm_batched_max_clusters(int32_t element, int32_t cluster, int64_t smem_bytes);
+/* dynamic shared memory of one patch-assembly CTA */
+int64_t tm_patch_smem_bytes(int32_t element, int32_t form, int32_t n_comp, int32_t dtype,
+                            const tm_patch_plan* plan, int32_t coef_kind, int32_t chunk);
+
+/*
  * Physical coordinates of every quadrature point, out[E][Q][D] =
  * sum_b N_b(xi_q) X[conn[e,b]] -- what the reference feeds to a ``func`` /
  * ``x`` argument (assemble/node_assembler.py:389, element_assembler.py:440).
@@ -180,10 +227,12 @@ int tm_spmv_csr(int32_t dtype, int64_t n_rows, const int64_t* indptr, const int3
  * 130-248 bicgstab_py).  Stops when ||r|| <= max(rtol*||b||, atol) on the
  * recurrence residual or after maxiter iterations.  x holds the initial guess
  * on entry.  work: caller-owned device scratch of at least
- * tm_pcg_workspace_bytes(dtype, n, tm_pcg_max_blocks(dtype)) bytes.
+ * tm_pcg_workspace_bytes(dtype, n, nnz, tm_pcg_max_blocks(dtype)) bytes.
+ * FP64 systems are iterated in double-float arithmetic on the FP32 pipe
+ * (values and vectors held as float pairs in the workspace).
  * Statuses of the solve itself are read back with tm_pcg_result.
  */
-int64_t tm_pcg_workspace_bytes(int32_t dtype, int64_t n, int32_t max_blocks);
+int64_t tm_pcg_workspace_bytes(int32_t dtype, int64_t n, int64_t nnz, int32_t max_blocks);
 int tm_pcg_max_blocks(int32_t dtype);
 int tm_pcg_jacobi(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
                   const void* values, const void* b, void* x, double rtol, double atol, int32_t maxiter,

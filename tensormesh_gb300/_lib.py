@@ -33,6 +33,7 @@ EXPORTS = [
     "tm_pcg_workspace_bytes", "tm_pcg_max_blocks", "tm_pcg_jacobi", "tm_pcg_result",
     "tm_csr_diagonal_inverse", "tm_gather", "tm_scatter", "tm_condense_rhs",
     "tm_assemble_backward", "tm_segment_sum",
+    "tm_batched_assemble_pcg", "tm_batched_max_clusters", "tm_patch_smem_bytes",
 ]
 
 P = ctypes.c_void_p
@@ -64,6 +65,19 @@ class BackwardArgs(ctypes.Structure):
     _fields_ = [("grad_out", P), ("pair_dX", P), ("pair_dcoef", P)]
 
 
+class BatchedArgs(ctypes.Structure):
+    _fields_ = [
+        ("element", ctypes.c_int32), ("cluster", ctypes.c_int32), ("n_clusters", ctypes.c_int32),
+        ("n_inst", ctypes.c_int32), ("maxiter", ctypes.c_int32), ("chunk", ctypes.c_int32),
+        ("rtol", ctypes.c_float), ("pad0", ctypes.c_int32),
+        ("n_rows", ctypes.c_int64), ("smem_bytes", ctypes.c_int64),
+        ("plan", ctypes.POINTER(PatchPlan)), ("mat", ctypes.POINTER(AssembleArgs)),
+        ("load", ctypes.POINTER(AssembleArgs)),
+        ("order", P), ("inst_pbeg", P), ("inst_rbeg", P), ("indices", P), ("dirichlet", P),
+        ("x", P), ("work", P), ("status", P), ("iters", P), ("resid", P), ("queue", P), ("stream", P),
+    ]
+
+
 class TensorMeshCudaError(RuntimeError):
     """A C-ABI call returned a non-zero status."""
 
@@ -92,8 +106,12 @@ def _declare(lib):
         "tm_assemble_backward": [ctypes.POINTER(PatchPlan), ctypes.POINTER(AssembleArgs),
                                  ctypes.POINTER(BackwardArgs), P],
         "tm_segment_sum": [i32, i64, P, P, i32, P, P, P],
+        "tm_batched_assemble_pcg": [ctypes.POINTER(BatchedArgs), P],
+        "tm_batched_max_clusters": [i32, i32, i64],
     }
-    lib.tm_pcg_workspace_bytes.argtypes = [i32, i64, i32]
+    lib.tm_patch_smem_bytes.argtypes = [i32, i32, i32, i32, ctypes.POINTER(PatchPlan), i32, i32]
+    lib.tm_patch_smem_bytes.restype = i64
+    lib.tm_pcg_workspace_bytes.argtypes = [i32, i64, i64, i32]
     lib.tm_pcg_workspace_bytes.restype = i64
     lib.tm_pcg_max_blocks.argtypes = [i32]
     lib.tm_pcg_max_blocks.restype = ctypes.c_int

@@ -95,13 +95,82 @@ TM_D void point_geometry(const R (&X)[B][D], const R* dNq /*[B][D]*/, R wq, R (&
   jxw = wq * Num<R>::abs(det);  // transformation.py:1289
 }
 
+// Closed-form P1 Laplace element matrix through the metric tensor.
+// With edge vectors d_k = x_k - x_0, G = D^T D, the cofactor vectors c_i of
+// J satisfy c_i . c_j = adj(G)_ij and |det J| = sqrt(det G), so
+//   K_ij = cW adj(G)_ij / |det J|   (i, j >= 1),   K_0j = -sum_i K_ij,
+// where cW = sum_q w_q c(x_q).  For a P1 simplex the gradients are constant,
+// so this equals the reference's quadrature sum of c gradu.gradv JxW
+// (assemble/builtin.py:62-63, element_assembler.py:211) for every order.
+template <int D, class R>
+TM_D void p1_laplace_closed_form(const R (&X)[D + 1][D], R cW, Strided<R> Ke) {
+  constexpr int B = D + 1;
+  R d[D][D];
+#pragma unroll
+  for (int k = 0; k < D; ++k)
+#pragma unroll
+    for (int c = 0; c < D; ++c) d[k][c] = X[k + 1][c] - X[0][c];
+  R G[D][D];
+#pragma unroll
+  for (int k = 0; k < D; ++k)
+#pragma unroll
+    for (int l = k; l < D; ++l) {
+      R s = d[k][0] * d[l][0];
+#pragma unroll
+      for (int c = 1; c < D; ++c) s = s + d[k][c] * d[l][c];
+      G[k][l] = s;
+      G[l][k] = s;
+    }
+  R A[D][D];  // adj(G)
+  R detG;
+  if constexpr (D == 2) {
+    A[0][0] = G[1][1];
+    A[1][1] = G[0][0];
+    A[0][1] = A[1][0] = -G[0][1];
+    detG = G[0][0] * G[1][1] - G[0][1] * G[0][1];
+  } else {
+    A[0][0] = G[1][1] * G[2][2] - G[1][2] * G[1][2];
+    A[1][1] = G[0][0] * G[2][2] - G[0][2] * G[0][2];
+    A[2][2] = G[0][0] * G[1][1] - G[0][1] * G[0][1];
+    A[0][1] = A[1][0] = G[0][2] * G[1][2] - G[0][1] * G[2][2];
+    A[0][2] = A[2][0] = G[0][1] * G[1][2] - G[0][2] * G[1][1];
+    A[1][2] = A[2][1] = G[0][1] * G[0][2] - G[0][0] * G[1][2];
+    detG = G[0][0] * A[0][0] + G[0][1] * A[0][1] + G[0][2] * A[0][2];
+  }
+  const R s = cW / Num<R>::sqrt(detG);
+  R k0[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      const R v = s * A[i][j];
+      Ke[(i + 1) * B + (j + 1)] = v;
+      Ke[(j + 1) * B + (i + 1)] = v;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    R t = Ke[1 * B + (j + 1)];
+#pragma unroll
+    for (int i = 1; i < D; ++i) t = t + Ke[(i + 1) * B + (j + 1)];
+    k0[j] = -t;
+    Ke[j + 1] = k0[j];
+    Ke[(j + 1) * B] = k0[j];
+  }
+  R t = k0[0];
+#pragma unroll
+  for (int j = 1; j < D; ++j) t = t + k0[j];
+  Ke[0] = -t;
+}
+
+// Assemble the rows owned by patch p (called by one CTA; nthreads = blockDim.x).
 template <int EL, int FORM, int H, class T, class R>
-__global__ void __launch_bounds__(kThreads)
-patch_assemble_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
+__device__ void assemble_patch(const tm_patch_plan& plan, const tm_assemble_args& args, const int p, const int chunk,
+                               unsigned char* smem_raw) {
   using L = Layout<EL, FORM, H>;
   constexpr int D = L::D, B = L::B, SE = L::SE, HH = L::HH;
-  const int p = blockIdx.x;
   const int tid = threadIdx.x;
+  const int kThreads = blockDim.x;
   const int Q = args.n_quad;
 
   const int vbeg = plan.vptr[p], nv = plan.vptr[p + 1] - vbeg;
@@ -109,7 +178,6 @@ patch_assemble_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
   const int rbeg = plan.rptr[p], nr = plan.rptr[p + 1] - rbeg;
   if (nr == 0) return;
 
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   R* s_tab = reinterpret_cast<R*>(smem_raw);                  // w, N, dN
   R* s_w = s_tab;
   R* s_N = s_w + kMaxQuad;
@@ -176,7 +244,24 @@ patch_assemble_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
       }
       R ce = scal[0];
       if (args.coef_kind == TM_COEF_ELEMENT) ce = tm_load<R, T>(coef[e]);
-      R* Ke = s_stage + (le - cbeg) * SE;
+      Strided<R> Ke{s_stage + (le - cbeg), chunk};
+      if constexpr (FORM == TM_FORM_LAPLACE && B == D + 1) {
+        R cW = Num<R>::zero();
+        for (int q = 0; q < Q; ++q) {
+          R cq = ce;
+          if (args.coef_kind == TM_COEF_POINT) {
+            R s = Num<R>::zero();
+#pragma unroll
+            for (int b = 0; b < B; ++b) s = s + s_pc[lv[b]] * s_N[q * B + b];
+            cq = s;
+          } else if (args.coef_kind == TM_COEF_QUAD) {
+            cq = tm_load<R, T>(coef[(int64_t)e * Q + q]);
+          }
+          cW = cW + s_w[q] * cq;
+        }
+        p1_laplace_closed_form<D, R>(X, cW, Ke);
+        continue;
+      }
       for (int i = 0; i < SE; ++i) Ke[i] = Num<R>::zero();
       for (int q = 0; q < Q; ++q) {
         R g[B][D], jxw;
@@ -236,14 +321,14 @@ patch_assemble_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
                 R dot = Num<R>::zero();
 #pragma unroll
                 for (int d = 0; d < D; ++d) dot = tm_fma_acc(dot, g[i][d], g[j][d]);
-                R* blk = Ke + (i * B + j) * HH;
+                const int base = (i * B + j) * HH;
 #pragma unroll
                 for (int a = 0; a < H; ++a)
 #pragma unroll
                   for (int b = 0; b < H; ++b) {
                     R v = lw * (g[i][a] * g[j][b]) + mw * (g[i][b] * g[j][a]);
                     if (a == b) v = v + mw * dot;
-                    blk[a * H + b] = blk[a * H + b] + v;
+                    Ke[base + a * H + b] = Ke[base + a * H + b] + v;
                   }
               }
           }
@@ -260,7 +345,7 @@ patch_assemble_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
         const int le = plan.inc_elem[cur];
         if (le >= cend) break;
         const int a = plan.inc_a[cur];
-        const R* Ke = s_stage + (le - cbeg) * SE;
+        const Strided<R> Ke{s_stage + (le - cbeg), chunk};
         if constexpr (L::kLoad) {
 #pragma unroll
           for (int h = 0; h < H; ++h) s_acc[ro + h] = s_acc[ro + h] + Ke[a * H + h];
@@ -269,9 +354,9 @@ patch_assemble_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
           for (int b = 0; b < B; ++b) {
             const int pos = plan.inc_pos[(int64_t)cur * B + b];
             R* dst = s_acc + ro + pos * HH;
-            const R* src = Ke + (a * B + b) * HH;
+            const int src = (a * B + b) * HH;
 #pragma unroll
-            for (int t = 0; t < HH; ++t) dst[t] = dst[t] + src[t];
+            for (int t = 0; t < HH; ++t) dst[t] = dst[t] + Ke[src + t];
           }
         }
         ++cur;
@@ -306,6 +391,13 @@ patch_assemble_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
       }
     }
   }
+}
+
+template <int EL, int FORM, int H, class T, class R>
+__global__ void __launch_bounds__(kThreads)
+patch_assemble_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  assemble_patch<EL, FORM, H, T, R>(plan, args, blockIdx.x, chunk, smem_raw);
 }
 
 // Shared-memory bytes needed by one CTA.

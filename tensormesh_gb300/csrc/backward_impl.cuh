@@ -45,7 +45,7 @@ patch_backward_kernel(tm_patch_plan plan, tm_assemble_args args, tm_backward_arg
   R* s_X = s_dN + kMaxQuad * B * D;
   R* s_pc = s_X + plan.max_vtx * D;
   const int pc_len = (args.coef_kind == TM_COEF_POINT) ? plan.max_vtx * (L::kLoad ? H : 1) : 0;
-  R* s_G = s_pc + pc_len;                          // staged dL/dK of owned rows [chunk][SE]
+  R* s_G = s_pc + pc_len;                          // staged dL/dK of owned rows [SE][chunk]
   int* s_cur = reinterpret_cast<int*>(s_G + chunk * SE);
 
   for (int i = tid; i < Q; i += kThreads) s_w[i] = Num<R>::from_double(args.tables[i]);
@@ -79,7 +79,7 @@ patch_backward_kernel(tm_patch_plan plan, tm_assemble_args args, tm_backward_arg
 
   for (int cbeg = 0; cbeg < ne; cbeg += chunk) {
     const int cend = min(ne, cbeg + chunk);
-    for (int i = tid; i < (cend - cbeg) * SE; i += kThreads) s_G[i] = Num<R>::zero();
+    for (int i = tid; i < chunk * SE; i += kThreads) s_G[i] = Num<R>::zero();
     __syncthreads();
     // --- phase B reversed: owned rows broadcast dL/dK into element slots ------
     for (int lr = tid; lr < nr; lr += kThreads) {
@@ -92,7 +92,7 @@ patch_backward_kernel(tm_patch_plan plan, tm_assemble_args args, tm_backward_arg
         const int le = plan.inc_elem[cur];
         if (le >= cend) break;
         const int a = plan.inc_a[cur];
-        R* Gs = s_G + (le - cbeg) * SE;
+        const Strided<R> Gs{s_G + (le - cbeg), chunk};
         if constexpr (L::kLoad) {
 #pragma unroll
           for (int h = 0; h < H; ++h) Gs[a * H + h] = tm_load<R, T>(G[(int64_t)r * H + h]);
@@ -126,7 +126,7 @@ patch_backward_kernel(tm_patch_plan plan, tm_assemble_args args, tm_backward_arg
 #pragma unroll
         for (int d = 0; d < D; ++d) X[b][d] = s_X[lv[b] * D + d];
       }
-      const R* S = s_G + (le - cbeg) * SE;
+      const Strided<R> S{s_G + (le - cbeg), chunk};
       R ce = scal[0];
       if (args.coef_kind == TM_COEF_ELEMENT) ce = tm_load<R, T>(coef[e]);
       R dX[B][D];
@@ -230,13 +230,13 @@ patch_backward_kernel(tm_patch_plan plan, tm_assemble_args args, tm_backward_arg
           for (int i = 0; i < B; ++i)
 #pragma unroll
             for (int j = 0; j < B; ++j) {
-              const R* Sb = S + (i * B + j) * HH;
+              const int sb = (i * B + j) * HH;
               R dot = Num<R>::zero();
 #pragma unroll
               for (int d = 0; d < D; ++d) dot = dot + P[i][d] * P[j][d];
               R tr = Num<R>::zero();
 #pragma unroll
-              for (int a = 0; a < H; ++a) tr = tr + Sb[a * H + a];
+              for (int a = 0; a < H; ++a) tr = tr + S[sb + a * H + a];
               phi = phi + mu1 * tr * dot;
 #pragma unroll
               for (int d = 0; d < D; ++d) {
@@ -247,7 +247,7 @@ patch_backward_kernel(tm_patch_plan plan, tm_assemble_args args, tm_backward_arg
               for (int a = 0; a < H; ++a)
 #pragma unroll
                 for (int b = 0; b < H; ++b) {
-                  const R s = Sb[a * H + b];
+                  const R s = S[sb + a * H + b];
                   phi = phi + s * (lam1 * (P[i][a] * P[j][b]) + mu1 * (P[i][b] * P[j][a]));
                   M[i][a] = M[i][a] + lam1 * s * P[j][b];
                   M[j][b] = M[j][b] + lam1 * s * P[i][a];

@@ -110,12 +110,17 @@ pcg_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restr
 
   // r = b - A x ; z = D^-1 r ; p = z ; partial rz, rr, bb
   T rz_l = 0, rr_l = 0, bb_l = 0;
-  for (int64_t row = r0 + g; row < r1; row += ngroups) {
+  // The trip count of every row loop below is uniform across the CTA, so all
+  // lanes reach each full-mask shuffle together.
+  for (int64_t base = r0; base < r1; base += ngroups) {
+    const int64_t row = base + g;
+    const bool valid = row < r1;
     T s = 0;
-    for (int64_t k = indptr[row] + lane; k < indptr[row + 1]; k += kGroup) s += val[k] * x[idx[k]];
+    if (valid)
+      for (int64_t k = indptr[row] + lane; k < indptr[row + 1]; k += kGroup) s += val[k] * x[idx[k]];
 #pragma unroll
     for (int o = kGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kGroup);
-    if (lane == 0) {
+    if (valid && lane == 0) {
       T rv = b[row] - s;
       T zv = dinv[row] * rv;
       r[row] = rv;
@@ -154,15 +159,18 @@ pcg_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restr
     if (it == maxiter) break;
     // q = A p_new, p_new = z + beta p_old formed on the fly; partial p.q
     T pq_l = 0;
-    for (int64_t row = r0 + g; row < r1; row += ngroups) {
+    for (int64_t base = r0; base < r1; base += ngroups) {
+      const int64_t row = base + g;
+      const bool valid = row < r1;
       T s = 0;
-      for (int64_t k = indptr[row] + lane; k < indptr[row + 1]; k += kGroup) {
-        const int c = idx[k];
-        s += val[k] * (z[c] + beta * pold[c]);
-      }
+      if (valid)
+        for (int64_t k = indptr[row] + lane; k < indptr[row + 1]; k += kGroup) {
+          const int c = idx[k];
+          s += val[k] * (z[c] + beta * pold[c]);
+        }
 #pragma unroll
       for (int o = kGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kGroup);
-      if (lane == 0) {
+      if (valid && lane == 0) {
         T pv = z[row] + beta * pold[row];
         q[row] = s;
         pq_l += pv * s;
@@ -207,6 +215,175 @@ pcg_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restr
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st->iters = it;
     st->res = sqrt((double)rr);
+    atomicCAS(&st->status, TM_OK, status);
+  }
+}
+
+// FP64 systems: values and vectors are held as double-float pairs (same bytes
+// as double) and every operation runs on the FP32 pipe; GB300's native FP64
+// FMA rate (~0.5 T/s) would otherwise bound the SpMV.
+struct F2 {
+  float hi, lo;
+};
+TM_D df64 ld2(const F2* a, int64_t i) {
+  F2 v = a[i];
+  return {v.hi, v.lo};
+}
+TM_D void st2(F2* a, int64_t i, df64 v) { a[i] = F2{v.hi, v.lo}; }
+
+__global__ void split_kernel(int64_t n, const double* __restrict__ src, F2* __restrict__ dst) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) {
+    df64 v = tm_from_double(src[i]);
+    dst[i] = F2{v.hi, v.lo};
+  }
+}
+
+__global__ void __launch_bounds__(kPcgThreads)
+pcg_df64_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ idx,
+                const F2* __restrict__ val, const double* __restrict__ bd, double* __restrict__ xd, F2* x, F2* r,
+                F2* z, F2* p0, F2* p1, F2* q, F2* dinv, double* partials, PcgState* st, double rtol, double atol,
+                int maxiter) {
+  __shared__ double s_red[32];
+  const unsigned nb = gridDim.x;
+  unsigned my_gen = 0;
+  const int64_t rows_per = (n + nb - 1) / nb;
+  const int64_t r0 = min(n, (int64_t)blockIdx.x * rows_per), r1 = min(n, r0 + rows_per);
+  const int g = threadIdx.x / kGroup, lane = threadIdx.x % kGroup;
+  const int ngroups = kPcgThreads / kGroup;
+  double* partA = partials;
+  double* partB = partials + nb;
+  double* partC = partials + 2 * nb;
+  const df64 zero{0.f, 0.f};
+
+  // diag^-1, x = x0, r = b - A x, z = D^-1 r, p = z
+  df64 rz_l = zero, rr_l = zero, bb_l = zero;
+  for (int64_t base = r0; base < r1; base += ngroups) {
+    const int64_t row = base + g;
+    const bool valid = row < r1;
+    df64 s = zero;
+    df64 d = {1.f, 0.f};
+    if (valid) {
+      for (int64_t k = indptr[row] + lane; k < indptr[row + 1]; k += kGroup) {
+        const int c = idx[k];
+        const df64 v = ld2(val, k);
+        if (c == row) d = v;
+        s += v * tm_from_double(xd[c]);
+      }
+    }
+    // the diagonal lives in exactly one lane of the group; find it
+    float dh = (d.hi != 1.f || d.lo != 0.f) ? 1.f : 0.f;
+#pragma unroll
+    for (int o = kGroup / 2; o > 0; o >>= 1) {
+      df64 t{__shfl_down_sync(0xffffffffu, s.hi, o, kGroup), __shfl_down_sync(0xffffffffu, s.lo, o, kGroup)};
+      s += t;
+    }
+    // broadcast the diagonal from the lane that saw it (or keep 1)
+    unsigned m = __ballot_sync(0xffffffffu, valid && dh != 0.f);
+    const unsigned grp_mask = 0xffu << ((threadIdx.x & 31) & ~(kGroup - 1));
+    const unsigned hit = m & grp_mask;
+    const int src = hit ? __ffs(hit) - 1 : ((threadIdx.x & 31) & ~(kGroup - 1));
+    df64 dd{__shfl_sync(0xffffffffu, d.hi, src), __shfl_sync(0xffffffffu, d.lo, src)};
+    if (valid && lane == 0) {
+      const df64 di = (dd.hi != 0.f) ? df64{1.f, 0.f} / dd : df64{1.f, 0.f};
+      const df64 bv = tm_from_double(bd[row]);
+      const df64 rv = bv - s;
+      const df64 zv = di * rv;
+      st2(dinv, row, di);
+      st2(x, row, tm_from_double(xd[row]));
+      st2(r, row, rv);
+      st2(z, row, zv);
+      st2(p0, row, zv);
+      rz_l += rv * zv;
+      rr_l += rv * rv;
+      bb_l += bv * bv;
+    }
+  }
+  double t = block_sum(tm_to_double(rz_l), s_red);
+  if (threadIdx.x == 0) partA[blockIdx.x] = t;
+  t = block_sum(tm_to_double(rr_l), s_red);
+  if (threadIdx.x == 0) partB[blockIdx.x] = t;
+  t = block_sum(tm_to_double(bb_l), s_red);
+  if (threadIdx.x == 0) partC[blockIdx.x] = t;
+  if (!grid_sync(st, nb, my_gen)) return;
+  double rz = sum_partials(partA, nb, s_red);
+  double rr = sum_partials(partB, nb, s_red);
+  const double bb = sum_partials(partC, nb, s_red);
+  const double bnorm = sqrt(bb);
+  const double tol = fmax(rtol * bnorm, atol);
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->bnorm = bnorm;
+  if (!grid_sync(st, nb, my_gen)) return;
+
+  df64 beta = zero;
+  F2* pold = p0;
+  F2* pnew = p1;
+  int it = 0;
+  int status = TM_ERR_MAXITER;
+  for (; it <= maxiter; ++it) {
+    if (sqrt(rr) <= tol) {
+      status = TM_OK;
+      break;
+    }
+    if (it == maxiter) break;
+    df64 pq_l = zero;
+    for (int64_t base = r0; base < r1; base += ngroups) {
+      const int64_t row = base + g;
+      const bool valid = row < r1;
+      df64 s = zero;
+      if (valid)
+        for (int64_t k = indptr[row] + lane; k < indptr[row + 1]; k += kGroup) {
+          const int c = idx[k];
+          s += ld2(val, k) * (ld2(z, c) + beta * ld2(pold, c));
+        }
+#pragma unroll
+      for (int o = kGroup / 2; o > 0; o >>= 1) {
+        df64 tt{__shfl_down_sync(0xffffffffu, s.hi, o, kGroup), __shfl_down_sync(0xffffffffu, s.lo, o, kGroup)};
+        s += tt;
+      }
+      if (valid && lane == 0) {
+        const df64 pv = ld2(z, row) + beta * ld2(pold, row);
+        st2(q, row, s);
+        pq_l += pv * s;
+      }
+    }
+    t = block_sum(tm_to_double(pq_l), s_red);
+    if (threadIdx.x == 0) partA[blockIdx.x] = t;
+    if (!grid_sync(st, nb, my_gen)) return;
+    const double pq = sum_partials(partA, nb, s_red);
+    if (!(pq > 0.0)) {
+      status = TM_ERR_BREAKDOWN;
+      break;
+    }
+    const df64 alpha = tm_from_double(rz / pq);
+    df64 rz_n = zero, rr_n = zero;
+    for (int64_t row = r0 + threadIdx.x; row < r1; row += kPcgThreads) {
+      const df64 pv = ld2(z, row) + beta * ld2(pold, row);
+      st2(pnew, row, pv);
+      st2(x, row, ld2(x, row) + alpha * pv);
+      const df64 rv = ld2(r, row) - alpha * ld2(q, row);
+      st2(r, row, rv);
+      const df64 zv = ld2(dinv, row) * rv;
+      st2(z, row, zv);
+      rz_n += rv * zv;
+      rr_n += rv * rv;
+    }
+    t = block_sum(tm_to_double(rz_n), s_red);
+    if (threadIdx.x == 0) partB[blockIdx.x] = t;
+    t = block_sum(tm_to_double(rr_n), s_red);
+    if (threadIdx.x == 0) partC[blockIdx.x] = t;
+    if (!grid_sync(st, nb, my_gen)) return;
+    const double rzn = sum_partials(partB, nb, s_red);
+    rr = sum_partials(partC, nb, s_red);
+    beta = tm_from_double(rzn / rz);
+    rz = rzn;
+    F2* tmp = pold;
+    pold = pnew;
+    pnew = tmp;
+  }
+  for (int64_t row = r0 + threadIdx.x; row < r1; row += kPcgThreads) xd[row] = tm_to_double(ld2(x, row));
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->iters = it;
+    st->res = sqrt(rr);
     atomicCAS(&st->status, TM_OK, status);
   }
 }
@@ -256,10 +433,11 @@ __global__ void scatter_kernel(int64_t n, const int64_t* __restrict__ map, const
 
 }  // namespace tmg
 
-extern "C" int64_t tm_pcg_workspace_bytes(int32_t dtype, int64_t n, int32_t max_blocks) {
-  const int64_t es = dtype == TM_F64 ? 8 : 4;
-  // state (256 B) | dinv r z p0 p1 q (6n) | partials (3 * blocks)
-  return 256 + es * (6 * n + 3 * (int64_t)max_blocks);
+extern "C" int64_t tm_pcg_workspace_bytes(int32_t dtype, int64_t n, int64_t nnz, int32_t max_blocks) {
+  if (dtype == TM_F64)  // state | 7 df64 vectors | df64 values | double partials
+    return 256 + 8 * (7 * n + nnz + 3 * (int64_t)max_blocks);
+  // state | dinv r z p0 p1 q (6n) | partials (3 * blocks)
+  return 256 + 4 * (6 * n + 3 * (int64_t)max_blocks);
 }
 
 extern "C" int tm_pcg_max_blocks(int32_t dtype) {
@@ -267,7 +445,7 @@ extern "C" int tm_pcg_max_blocks(int32_t dtype) {
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (dtype == TM_F64)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tmg::pcg_kernel<double>, tmg::kPcgThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tmg::pcg_df64_kernel, tmg::kPcgThreads, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tmg::pcg_kernel<float>, tmg::kPcgThreads, 0);
   return sms * (per_sm > 2 ? 2 : per_sm);
@@ -296,6 +474,28 @@ static int launch_pcg(int64_t n, const int64_t* indptr, const int32_t* indices, 
   return e == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
 
+static int launch_pcg_df64(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values,
+                           const double* b, double* x, double rtol, double atol, int maxiter, char* w, int nb,
+                           cudaStream_t s) {
+  int64_t nnz = 0;
+  if (cudaMemcpyAsync(&nnz, indptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess) return TM_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return TM_ERR_CUDA;
+  tmg::PcgState* st = reinterpret_cast<tmg::PcgState*>(w);
+  tmg::F2* base = reinterpret_cast<tmg::F2*>(w + 256);
+  tmg::F2 *xv = base, *r = base + n, *z = base + 2 * n, *p0 = base + 3 * n, *p1 = base + 4 * n, *q = base + 5 * n,
+          *dinv = base + 6 * n, *val = base + 7 * n;
+  double* partials = reinterpret_cast<double*>(val + nnz);
+  if (cudaMemsetAsync(st, 0, sizeof(tmg::PcgState), s) != cudaSuccess) return TM_ERR_CUDA;
+  if (nnz > 0) tmg::split_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, values, val);
+  const tmg::F2* cval = val;
+  void* args[] = {(void*)&n, (void*)&indptr, (void*)&indices, (void*)&cval, (void*)&b, (void*)&x, (void*)&xv,
+                  (void*)&r, (void*)&z, (void*)&p0, (void*)&p1, (void*)&q, (void*)&dinv, (void*)&partials,
+                  (void*)&st, (void*)&rtol, (void*)&atol, (void*)&maxiter};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void*)tmg::pcg_df64_kernel, dim3(nb), dim3(tmg::kPcgThreads),
+                                              args, 0, s);
+  return e == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
 extern "C" int tm_pcg_jacobi(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
                              const void* values, const void* b, void* x, double rtol, double atol, int32_t maxiter,
                              void* work, int64_t work_bytes, void* stream) {
@@ -304,12 +504,18 @@ extern "C" int tm_pcg_jacobi(int32_t dtype, int64_t n, const int64_t* indptr, co
   if (!indptr || !indices || !values || !b || !x || !work) return TM_ERR_INVALID;
   const int nb = tm_pcg_max_blocks(dtype);
   if (nb <= 0) return TM_ERR_CUDA;
-  if (work_bytes < tm_pcg_workspace_bytes(dtype, n, nb)) return TM_ERR_INDEX;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   char* w = static_cast<char*>(work);
-  if (dtype == TM_F64)
-    return launch_pcg<double>(n, indptr, indices, (const double*)values, (const double*)b, (double*)x, rtol, atol,
-                              maxiter, w, nb, s);
+  if (dtype == TM_F64) {
+    int64_t nnz = 0;
+    if (cudaMemcpyAsync(&nnz, indptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      return TM_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return TM_ERR_CUDA;
+    if (work_bytes < tm_pcg_workspace_bytes(dtype, n, nnz, nb)) return TM_ERR_INDEX;
+    return launch_pcg_df64(n, indptr, indices, (const double*)values, (const double*)b, (double*)x, rtol, atol,
+                           maxiter, w, nb, s);
+  }
+  if (work_bytes < tm_pcg_workspace_bytes(dtype, n, 0, nb)) return TM_ERR_INDEX;
   if (dtype == TM_F32)
     return launch_pcg<float>(n, indptr, indices, (const float*)values, (const float*)b, (float*)x, rtol, atol,
                              maxiter, w, nb, s);

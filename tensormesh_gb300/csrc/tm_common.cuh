@@ -119,3 +119,13 @@ template <class T, class R> TM_D T tm_store(R v);
 template <> TM_D float tm_store<float, float>(float v) { return v; }
 template <> TM_D double tm_store<double, double>(double v) { return v; }
 template <> TM_D double tm_store<double, df64>(df64 v) { return tm_to_double(v); }
+
+// Strided view of a staging slot: element-major slots are laid out
+// structure-of-arrays ([entry][element]) so that the threads of a warp, each
+// working on its own element, touch consecutive shared-memory words.
+template <class R>
+struct Strided {
+  R* p;
+  int s;
+  TM_D R& operator[](int i) const { return p[i * s]; }
+};

@@ -115,11 +115,48 @@ def rcb_partition(coords: torch.Tensor, n_levels: int) -> torch.Tensor:
     return part
 
 
+def rcb_partition_grouped(coords: torch.Tensor, groups: torch.Tensor, weight: torch.Tensor,
+                          budget: float, max_rows: int):
+    """RCB inside fixed groups (e.g. the instances of a batch): segments start
+    as the groups and are bisected along their longest extent until each
+    holds at most ``budget`` weight (CSR slots) and ``max_rows`` points.
+    Parts never straddle groups; part ids are dense and ordered by group."""
+    N = coords.shape[0]
+    dev = coords.device
+    c = coords.to(torch.float64)
+    D = c.shape[1]
+    seg = groups.long().clone()
+    ar = torch.arange(N, device=dev)
+    w = weight.to(torch.float64)
+    for _ in range(64):
+        nseg = int(seg.max()) + 1 if N else 0
+        cnt = torch.bincount(seg, minlength=nseg)
+        wsum = torch.zeros(nseg, dtype=torch.float64, device=dev).index_add_(0, seg, w)
+        split = (wsum > budget) | (cnt > max_rows)
+        split &= cnt > 1
+        if not bool(split.any()):
+            break
+        idx = seg.unsqueeze(1).expand(N, D)
+        mx = torch.full((nseg, D), -math.inf, dtype=torch.float64, device=dev).scatter_reduce(0, idx, c, "amax")
+        mn = torch.full((nseg, D), math.inf, dtype=torch.float64, device=dev).scatter_reduce(0, idx, c, "amin")
+        axis = torch.argmax(mx - mn, dim=1)
+        val = c[ar, axis[seg]]
+        o1 = torch.argsort(val, stable=True)
+        order = o1[torch.argsort(seg[o1], stable=True)]
+        start = torch.cumsum(cnt, 0) - cnt
+        pos = torch.empty(N, dtype=torch.int64, device=dev)
+        pos[order] = ar - start[seg[order]]
+        side = ((pos >= (cnt[seg] + 1) // 2) & split[seg]).long()
+        seg = 2 * seg + side
+    _, part = torch.unique(seg, sorted=True, return_inverse=True)
+    return part
+
+
 class PatchPlan:
     """Device arrays of the patch structure plus the ctypes view of them."""
 
     def __init__(self, elements: torch.Tensor, coords: torch.Tensor, pattern: NodePattern,
-                 slot_budget: int = 6144, max_rows_cap: int = 2048):
+                 slot_budget: int = 6144, max_rows_cap: int = 2048, groups: torch.Tensor = None):
         dev = elements.device
         E, B = elements.shape
         N = pattern.n_points
@@ -131,17 +168,26 @@ class PatchPlan:
             raise NotImplementedError("a CSR row longer than 255 entries is not supported by the patch plan")
 
         # -- partition: enough RCB levels that every patch fits the slot budget
-        avg_deg = float(deg.float().mean()) if N else 1.0
-        target_rows = max(16, min(max_rows_cap, int(slot_budget / max(avg_deg, 1.0))))
-        n_levels = max(0, math.ceil(math.log2(max(1, N) / target_rows)))
-        while True:
-            part = rcb_partition(coords, n_levels) if N else torch.zeros(0, dtype=torch.int64, device=dev)
-            n_parts = 1 << n_levels
+        if groups is not None:
+            part = rcb_partition_grouped(coords, groups, deg, slot_budget, max_rows_cap)
+            n_parts = int(part.max()) + 1 if N else 0
             slots_per_part = torch.zeros(n_parts, dtype=torch.int64, device=dev).index_add_(0, part, deg)
             rows_per_part = torch.bincount(part, minlength=n_parts)
-            if N == 0 or (int(slots_per_part.max()) <= 2 * slot_budget and int(rows_per_part.max()) <= max_rows_cap):
-                break
-            n_levels += 1
+            self.part = part
+        else:
+            avg_deg = float(deg.float().mean()) if N else 1.0
+            target_rows = max(16, min(max_rows_cap, int(slot_budget / max(avg_deg, 1.0))))
+            n_levels = max(0, math.ceil(math.log2(max(1, N) / target_rows)))
+            while True:
+                part = rcb_partition(coords, n_levels) if N else torch.zeros(0, dtype=torch.int64, device=dev)
+                n_parts = 1 << n_levels
+                slots_per_part = torch.zeros(n_parts, dtype=torch.int64, device=dev).index_add_(0, part, deg)
+                rows_per_part = torch.bincount(part, minlength=n_parts)
+                if N == 0 or (int(slots_per_part.max()) <= 2 * slot_budget and
+                              int(rows_per_part.max()) <= max_rows_cap):
+                    break
+                n_levels += 1
+            self.part = part
         self.n_patches = n_parts
 
         # -- owned rows, sorted by (patch, node id)

@@ -90,25 +90,25 @@ def csr_diagonal(A) -> torch.Tensor:
 class PCGWorkspace:
     """Device scratch for tm_pcg_jacobi, reused across solves of one size."""
 
-    def __init__(self, n: int, dtype: torch.dtype, device):
+    def __init__(self, n: int, nnz: int, dtype: torch.dtype, device):
         lib = _lib.load()
         code = _lib.TM_F64 if dtype == torch.float64 else _lib.TM_F32
         self.max_blocks = lib.tm_pcg_max_blocks(code)
-        self.nbytes = int(lib.tm_pcg_workspace_bytes(code, n, self.max_blocks))
+        self.nbytes = int(lib.tm_pcg_workspace_bytes(code, n, nnz, self.max_blocks))
         self.buf = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
-        self.n, self.dtype = n, dtype
+        self.n, self.nnz, self.dtype = n, nnz, dtype
 
 
 _WS = {}
 
 
-def workspace(n, dtype, device) -> PCGWorkspace:
-    key = (n, dtype, str(device))
+def workspace(n, nnz, dtype, device) -> PCGWorkspace:
+    key = (n, nnz, dtype, str(device))
     ws = _WS.get(key)
     if ws is None:
         if len(_WS) > 4:
             _WS.clear()
-        ws = _WS[key] = PCGWorkspace(n, dtype, device)
+        ws = _WS[key] = PCGWorkspace(n, nnz, dtype, device)
     return ws
 
 
@@ -116,7 +116,7 @@ def pcg_jacobi_raw(indptr, indices, values, b, x, rtol=1e-8, atol=0.0, maxiter=1
     """Solve in place into x; returns SolveInfo."""
     n = b.shape[0]
     dev = values.device
-    ws = workspace(n, values.dtype, dev)
+    ws = workspace(n, int(values.shape[0]), values.dtype, dev)
     s = _lib.stream_handle(dev)
     code = _dt(values)
     bnorm = float(torch.linalg.vector_norm(b.double()))
