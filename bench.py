@@ -270,10 +270,10 @@ def run_ours(args):
         K = asm(mesh.points, element_data={"kappa": kappa})
         b = tg.const_node_assembler(1.0).from_mesh(mesh, quadrature_order=1)(mesh.points)
         K_ii, f_i = tg.Condenser(mesh.boundary_mask)(K, b)
-        K_ii.solve(f_i, rtol=1e-8, maxiter=200000)  # warm (workspace, launch)
+        K_ii.solve(f_i, rtol=1e-8, maxiter=args.pcg_maxiter)  # warm (workspace, launch)
         torch.cuda.synchronize()
         ta = time.perf_counter()
-        K_ii.solve(f_i, rtol=1e-8, maxiter=200000)
+        K_ii.solve(f_i, rtol=1e-8, maxiter=args.pcg_maxiter)
         torch.cuda.synchronize()
         tb = time.perf_counter()
         info = K_ii.last_solve_info
@@ -321,14 +321,18 @@ def run_ours(args):
 
 
 def main():
+    global N_CELLS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-pcg", action="store_true")
+    ap.add_argument("--cube", type=int, default=N_CELLS, help="cells per side (profiling runs use smaller cubes)")
+    ap.add_argument("--pcg-maxiter", type=int, default=200000)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
+    N_CELLS = args.cube
     if args.impl == "reference":
         run_reference(args)
     else:

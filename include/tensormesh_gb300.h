@@ -255,6 +255,37 @@ int tm_condense_rhs(int32_t dtype, int64_t n_inner, const int64_t* inner_dof, co
                     const int64_t* io_indptr, const int32_t* io_indices, const void* io_values,
                     const void* u_outer, void* out, void* stream);
 
+/*
+ * Message-passing network of the learned preconditioner (hidden width 64,
+ * BF16 features/weights on the tensor cores via mma.sync, FP32 accumulate).
+ * Graph = CSR pattern of the condensed matrix with normalised off-diagonal
+ * weights aoff (float32, 0 on the diagonal).  Features are row-major [n][64]
+ * bf16.  No reference counterpart exists: the reference has no learned
+ * preconditioner; these kernels serve the flexible-PCG path that replaces
+ * K.solve (torch_sla) for the 128^3 configuration.
+ *   input_fwd : H0 = relu(x w[0] + (A x) w[1] + w[2]), y = A x
+ *   layer_fwd : Hout = act([Hin | A Hin] Wt^T + b), Wt = [64 out][128 in]
+ *   readout   : out = scale * (H wr[0:64] + A (H wr[64:128]))
+ * Backward kernels return dH and fixed-order reduced weight gradients.
+ */
+int tm_mpnn_input_fwd(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff,
+                      const float* x, const float* w, void* H0, float* y, void* stream);
+int tm_mpnn_layer_fwd(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff,
+                      const void* Hin, const void* Wt, const float* bias, void* Hout, int32_t relu, void* stream);
+int tm_mpnn_readout_fwd(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff, const void* H,
+                        const float* wr, const float* scale, float* u, float* t, float* out, void* stream);
+int tm_mpnn_readout_bwd(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff, const void* H,
+                        const float* g, const float* wr, float* dH, float* part, float* dwr, void* stream);
+int tm_mpnn_layer_bwd(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff,
+                      const void* Hin, const void* Hout, const float* dHout, const void* W, int32_t relu,
+                      float* part_dW, float* part_db, float* U, float* T, float* dHin, float* dW, float* db,
+                      void* stream);
+int tm_mpnn_input_bwd(int64_t n, const float* x, const float* y, const void* H0, const float* dH0, float* part,
+                      float* dw, void* stream);
+/* out = scale * (u + A t) over a float32 CSR (u, scale may be NULL) */
+int tm_gather_axpy_f32(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff,
+                       const float* u, const float* t, const float* scale, float* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,8 @@ EXPORTS = [
     "tm_csr_diagonal_inverse", "tm_gather", "tm_scatter", "tm_condense_rhs",
     "tm_assemble_backward", "tm_segment_sum",
     "tm_batched_assemble_pcg", "tm_batched_max_clusters", "tm_patch_smem_bytes",
+    "tm_mpnn_input_fwd", "tm_mpnn_layer_fwd", "tm_mpnn_readout_fwd", "tm_mpnn_readout_bwd",
+    "tm_mpnn_layer_bwd", "tm_mpnn_input_bwd", "tm_gather_axpy_f32",
 ]
 
 P = ctypes.c_void_p
@@ -108,6 +110,13 @@ def _declare(lib):
         "tm_segment_sum": [i32, i64, P, P, i32, P, P, P],
         "tm_batched_assemble_pcg": [ctypes.POINTER(BatchedArgs), P],
         "tm_batched_max_clusters": [i32, i32, i64],
+        "tm_mpnn_input_fwd": [i64, P, P, P, P, P, P, P, P],
+        "tm_mpnn_layer_fwd": [i64, P, P, P, P, P, P, P, i32, P],
+        "tm_mpnn_readout_fwd": [i64, P, P, P, P, P, P, P, P, P, P],
+        "tm_mpnn_readout_bwd": [i64, P, P, P, P, P, P, P, P, P, P],
+        "tm_mpnn_layer_bwd": [i64, P, P, P, P, P, P, P, i32, P, P, P, P, P, P, P, P],
+        "tm_mpnn_input_bwd": [i64, P, P, P, P, P, P, P],
+        "tm_gather_axpy_f32": [i64, P, P, P, P, P, P, P, P],
     }
     lib.tm_patch_smem_bytes.argtypes = [i32, i32, i32, i32, ctypes.POINTER(PatchPlan), i32, i32]
     lib.tm_patch_smem_bytes.restype = i64
