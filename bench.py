@@ -228,6 +228,53 @@ def run_ours(args):
     ms_per_step = total_ms / args.steps
     value = world * E / (ms_per_step * 1e-3)
 
+    # ---- float32 variant of the same assembly (secondary line item)
+    def time_calls(fn, reps=5):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b_ = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b_.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b_) / reps
+
+    fp32 = None
+    if not args.no_extra:
+        pts32 = mesh.points.float().contiguous()
+        kap32 = kappa.float()
+        ms32 = time_calls(lambda: asm(pts32, element_data={"kappa": kap32}))
+        alg32 = algorithmic_bytes(E, B, D, N, nnz, itemsize=4)
+        fp32 = {"elements_per_s": E / (ms32 * 1e-3), "kernel_ms": ms32, "algorithmic_bytes": alg32,
+                "achieved_gbs": alg32 / (ms32 * 1e-3) / 1e9}
+        peaks_path_ = os.path.join(ROOT, "MEASURED_PEAKS.json")
+        if os.path.exists(peaks_path_):
+            fp32["hbm_frac"] = fp32["achieved_gbs"] / float(json.load(open(peaks_path_))["hbm_gbs"])
+
+    # ---- C2: 64^3 P1-tet linear elasticity, per-element E, FP64 (secondary)
+    elast = None
+    if not args.no_extra:
+        m2 = tg.Mesh.gen_unit_cube(64, device=dev)
+        rng = np.random.default_rng(SEED + 2)
+        Emod = torch.from_numpy(np.exp(0.5 * rng.normal(size=m2.n_elements))).to(dev)
+
+        class EElast(tg.ElementAssembler):
+            def forward(self, gradu, gradv, E):
+                lam, mu = tg.forms.reference_lame(1.0, 0.3)
+                return E * tg.forms.elasticity_block(gradu, gradv, lam, mu)
+        easm = EElast.from_mesh(m2, quadrature_order=1)
+        ms2 = time_calls(lambda: easm(m2.points, element_data={"E": Emod}), reps=3)
+        t2 = easm.topology
+        dnnz = 9 * t2.pattern.nnz
+        alg2 = 4 * 4 * t2.n_elements + 8 * 3 * t2.n_points + 8 * t2.n_elements + 8 * dnnz
+        elast = {"workload": "64^3 Kuhn cube P1-tet elasticity, per-element E = exp(0.5 g), nu = 0.3, FP64",
+                 "elements_per_s": t2.n_elements / (ms2 * 1e-3), "kernel_ms": ms2, "algorithmic_bytes": alg2,
+                 "achieved_gbs": alg2 / (ms2 * 1e-3) / 1e9}
+        del easm, m2
+
     # ---- end to end through the public API with host buffers
     pts_h = mesh.points.cpu().pin_memory()
     kap_h = kappa_h.pin_memory()
@@ -282,6 +329,29 @@ def run_ours(args):
                "status": info.status, "n": K_ii.shape[0], "nnz": K_ii.nnz,
                "per_iteration_algorithmic_bytes": it_bytes,
                "achieved_gbs": it_bytes * info.iterations / (tb - ta) / 1e9, "learned_seconds_to_1e-8": None}
+        wpath = os.path.join(ROOT, "tensormesh_gb300", "weights", "mpnn_poisson_kuhn32.npz")
+        if os.path.exists(wpath) and not args.no_learned:
+            from tensormesh_gb300.learned import LearnedPreconditioner
+            from tensormesh_gb300.train_learned import load_weights
+            coords = mesh.points[~mesh.boundary_mask].contiguous()
+            pre = LearnedPreconditioner(load_weights(wpath, dev), coarse_target=512)
+            torch.cuda.synchronize()
+            t0s = time.perf_counter()
+            pre.setup(K_ii, coords)
+            torch.cuda.synchronize()
+            t_setup = time.perf_counter() - t0s
+            x = torch.zeros_like(f_i)
+            pre.solve(K_ii, f_i, x.clone(), rtol=1e-8, coords=coords, maxiter=2000)  # warm
+            torch.cuda.synchronize()
+            t0s = time.perf_counter()
+            linfo = pre.solve(K_ii, f_i, x, rtol=1e-8, coords=coords, maxiter=2000)
+            torch.cuda.synchronize()
+            t_solve = time.perf_counter() - t0s
+            pcg.update({"learned_seconds_to_1e-8": t_solve, "learned_setup_seconds": t_setup,
+                        "learned_iterations": linfo.iterations, "learned_true_residual": linfo.residual,
+                        "learned_status": linfo.status, "learned_fallback": linfo.fallback,
+                        "learned_vs_jacobi_time_ratio": (t_solve + t_setup) / (tb - ta),
+                        "learned_vs_jacobi_time_ratio_solve_only": t_solve / (tb - ta)})
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -311,6 +381,8 @@ def run_ours(args):
             "e2e": {"value": world * E / (e2e_ms * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
             "cpu_baseline": cpu,
+            "fp32_variant": fp32,
+            "elasticity_c2": elast,
             "gpu_launches": args.steps,
             "clocks": clk,
             "pcg": pcg,
@@ -330,6 +402,8 @@ def main():
     ap.add_argument("--no-pcg", action="store_true")
     ap.add_argument("--cube", type=int, default=N_CELLS, help="cells per side (profiling runs use smaller cubes)")
     ap.add_argument("--pcg-maxiter", type=int, default=200000)
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the float32 and elasticity side measurements")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     N_CELLS = args.cube

@@ -2,9 +2,12 @@
 // TM_TET4 (one translation unit per element type so the build compiles them
 // in parallel).
 #include "backward_impl.cuh"
+#include "p1tet_fast.cuh"
 
 namespace tmg {
 int assemble_tet4(const tm_patch_plan& plan, const tm_assemble_args& a, cudaStream_t s) {
+  if (a.form == TM_FORM_LAPLACE && a.dtype == TM_F64 && a.precision == TM_PREC_EMULATED)
+    return launch_p1tet_laplace_df64(plan, a, s);
   return assemble_element<TM_TET4>(plan, a, s);
 }
 int backward_tet4(const tm_patch_plan& plan, const tm_assemble_args& a, const tm_backward_args& bw, cudaStream_t s) {

@@ -1,0 +1,267 @@
+// Specialised FP64 path for the headline case: P1 tetrahedra, Laplace form
+// with a per-element (or scalar / interpolated) coefficient, emulated FP64.
+//
+// Same patch decomposition and deterministic row-owner accumulation as the
+// generic kernel (assemble_impl.cuh), with the arithmetic cut to what the
+// 1e-12 bar needs:
+//   * "lazy" double-float values (hi, lo) whose lo part is not renormalised
+//     after every operation (error-free products by FMA, TwoSum only where
+//     two leading parts are added);
+//   * 1/sqrt(det G) from the MUFU estimate plus one Newton step carried out
+//     in double-float, instead of IEEE division and square root;
+//   * the 10 unique entries of the symmetric element matrix are staged (not
+//     16).
+#pragma once
+#include "assemble_impl.cuh"
+
+namespace tmg {
+
+struct L2 {  // lazy double-float: value = h + l, |l| << |h|
+  float h, l;
+};
+
+TM_D L2 l2_from(df64 a) { return {a.hi, a.lo}; }
+TM_D L2 l2_sub(L2 a, L2 b) {
+  const float s = __fsub_rn(a.h, b.h);
+  const float bb = __fsub_rn(s, a.h);
+  const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(-b.h, bb));
+  return {s, __fadd_rn(e, __fsub_rn(a.l, b.l))};
+}
+TM_D L2 l2_add(L2 a, L2 b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float bb = __fsub_rn(s, a.h);
+  const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+  return {s, __fadd_rn(e, __fadd_rn(a.l, b.l))};
+}
+TM_D L2 l2_mul(L2 a, L2 b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return {p, e};
+}
+TM_D L2 l2_neg(L2 a) { return {-a.h, -a.l}; }
+TM_D L2 l2_norm(L2 a) {
+  const float s = __fadd_rn(a.h, a.l);
+  return {s, __fsub_rn(a.l, __fsub_rn(s, a.h))};
+}
+// dot of two 3-vectors
+TM_D L2 l2_dot3(const L2* a, const L2* b) {
+  return l2_add(l2_add(l2_mul(a[0], b[0]), l2_mul(a[1], b[1])), l2_mul(a[2], b[2]));
+}
+// a*b - c*d
+TM_D L2 l2_cof(L2 a, L2 b, L2 c, L2 d) { return l2_sub(l2_mul(a, b), l2_mul(c, d)); }
+
+// 1/sqrt(x) for x > 0: MUFU estimate, one Newton step in double-float
+// (y1 = y0 + y0 (1 - x y0^2) / 2; the residual 1 - x y0^2 is formed with
+// error-free products so the step doubles the ~22 correct bits).
+TM_D L2 l2_rsqrt(L2 x) {
+  x = l2_norm(x);
+  const float y0 = rsqrtf(x.h);
+  const float y2 = __fmul_rn(y0, y0);
+  const float y2e = __fmaf_rn(y0, y0, -y2);           // y0^2 = y2 + y2e exactly
+  L2 t = l2_mul(x, L2{y2, y2e});                       // x y0^2
+  t = l2_norm(t);
+  const float r = __fadd_rn(__fsub_rn(1.0f, t.h), -t.l);  // 1 - x y0^2 (small)
+  const float corr = __fmul_rn(__fmul_rn(0.5f, y0), r);
+  return l2_norm(L2{y0, corr});
+}
+
+// Unique-entry index of (a, b) in the staged upper triangle of a 4x4:
+// (0,0)0 (0,1)1 (0,2)2 (0,3)3 (1,1)4 (1,2)5 (1,3)6 (2,2)7 (2,3)8 (3,3)9
+TM_D int tri4(int a, int b) {
+  const int i = a < b ? a : b, j = a < b ? b : a;
+  return i * 4 - (i * (i - 1)) / 2 + (j - i);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads)
+p1tet_laplace_df64_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
+  const int p = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int Q = args.n_quad;
+  const int vbeg = plan.vptr[p], nv = plan.vptr[p + 1] - vbeg;
+  const int ebeg = plan.eptr[p], ne = plan.eptr[p + 1] - ebeg;
+  const int rbeg = plan.rptr[p], nr = plan.rptr[p + 1] - rbeg;
+  if (nr == 0) return;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* s_X = reinterpret_cast<float2*>(smem_raw);              // [max_vtx][3]
+  float2* s_pc = s_X + plan.max_vtx * 3;                           // [max_vtx] point coef
+  const int pc_len = args.coef_kind == TM_COEF_POINT ? plan.max_vtx : 0;
+  float2* s_acc = s_pc + pc_len;                                   // [max_slots]
+  float2* s_stage = s_acc + plan.max_slots;                        // [10][chunk]
+  int* s_cur = reinterpret_cast<int*>(s_stage + 10 * chunk);       // [max_rows] incidence cursors
+
+  const T* pts = static_cast<const T*>(args.points);
+  for (int i = tid; i < nv * 3; i += kThreads) {
+    const int v = plan.vtx[vbeg + i / 3];
+    const df64 x = tm_from_double(pts[(int64_t)v * 3 + i % 3]);
+    s_X[i] = make_float2(x.hi, x.lo);
+  }
+  const T* coef = static_cast<const T*>(args.coef);
+  if (args.coef_kind == TM_COEF_POINT) {
+    for (int i = tid; i < nv; i += kThreads) {
+      const df64 c = tm_from_double(coef[plan.vtx[vbeg + i]]);
+      s_pc[i] = make_float2(c.hi, c.lo);
+    }
+  }
+  {
+    const int lr = rbeg + nr - 1;
+    const int r = plan.rows[lr];
+    const int total = plan.racc[lr] + (int)(plan.indptr[r + 1] - plan.indptr[r]);
+    for (int i = tid; i < total; i += kThreads) s_acc[i] = make_float2(0.f, 0.f);
+  }
+  for (int i = tid; i < nr; i += kThreads) s_cur[i] = plan.iptr[rbeg + i];
+  // quadrature weight sum and (for point/quad coefficients) shape values
+  double wsum = 0.0;
+  for (int q = 0; q < Q; ++q) wsum += args.tables[q];
+  const df64 Wd = tm_from_double(wsum);
+  const L2 W{Wd.hi, Wd.lo};
+  const df64 sc = tm_from_double(args.scal[0]);
+  __syncthreads();
+
+  // row-owner state kept across chunks: the thread's rows are tid, tid+256, ...
+  for (int cbeg = 0; cbeg < ne; cbeg += chunk) {
+    const int cend = min(ne, cbeg + chunk);
+    // --- phase A -------------------------------------------------------------
+    for (int le = cbeg + tid; le < cend; le += kThreads) {
+      const int pair = ebeg + le;
+      const uint2 cw = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)pair * 4);
+      const int lv[4] = {(int)(cw.x & 0xffff), (int)(cw.x >> 16), (int)(cw.y & 0xffff), (int)(cw.y >> 16)};
+      L2 X[4][3];
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const float2 v = s_X[lv[b] * 3 + d];
+          X[b][d] = L2{v.x, v.y};
+        }
+      L2 c;
+      if (args.coef_kind == TM_COEF_ELEMENT) {
+        c = l2_from(tm_from_double(coef[plan.elem[pair]]));
+      } else if (args.coef_kind == TM_COEF_POINT) {
+        // sum_q w_q sum_b N_b(q) c_b / W : P1 -> weighted vertex average
+        double cw_ = 0.0;
+        for (int q = 0; q < Q; ++q)
+          for (int b = 0; b < 4; ++b) {
+            const float2 pc = s_pc[lv[b]];
+            cw_ += args.tables[q] * args.tables[Q + q * 4 + b] * ((double)pc.x + (double)pc.y);
+          }
+        c = l2_from(tm_from_double(cw_ / wsum));
+      } else if (args.coef_kind == TM_COEF_QUAD) {
+        double cw_ = 0.0;
+        for (int q = 0; q < Q; ++q) cw_ += args.tables[q] * (double)coef[(int64_t)plan.elem[pair] * Q + q];
+        c = l2_from(tm_from_double(cw_ / wsum));
+      } else {
+        c = l2_from(sc);
+      }
+      L2 d[3][3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd) d[k][dd] = l2_sub(X[k + 1][dd], X[0][dd]);
+      const L2 G00 = l2_dot3(d[0], d[0]), G11 = l2_dot3(d[1], d[1]), G22 = l2_dot3(d[2], d[2]);
+      const L2 G01 = l2_dot3(d[0], d[1]), G02 = l2_dot3(d[0], d[2]), G12 = l2_dot3(d[1], d[2]);
+      const L2 A00 = l2_cof(G11, G22, G12, G12), A11 = l2_cof(G00, G22, G02, G02), A22 = l2_cof(G00, G11, G01, G01);
+      const L2 A01 = l2_cof(G02, G12, G01, G22), A02 = l2_cof(G01, G12, G02, G11), A12 = l2_cof(G01, G02, G00, G12);
+      const L2 detG = l2_add(l2_add(l2_mul(G00, A00), l2_mul(G01, A01)), l2_mul(G02, A02));
+      const L2 s = l2_mul(l2_mul(c, W), l2_rsqrt(detG));
+      const L2 k11 = l2_mul(s, A00), k22 = l2_mul(s, A11), k33 = l2_mul(s, A22);
+      const L2 k12 = l2_mul(s, A01), k13 = l2_mul(s, A02), k23 = l2_mul(s, A12);
+      const L2 k01 = l2_neg(l2_add(l2_add(k11, k12), k13));
+      const L2 k02 = l2_neg(l2_add(l2_add(k12, k22), k23));
+      const L2 k03 = l2_neg(l2_add(l2_add(k13, k23), k33));
+      const L2 k00 = l2_neg(l2_add(l2_add(k01, k02), k03));
+      const int lo = le - cbeg;
+      const L2 vals[10] = {k00, k01, k02, k03, k11, k12, k13, k22, k23, k33};
+#pragma unroll
+      for (int u = 0; u < 10; ++u) s_stage[u * chunk + lo] = make_float2(vals[u].h, vals[u].l);
+    }
+    __syncthreads();
+    // --- phase B: rows gather their incidences (fixed order) -----------------
+    // The diagonal of the row is summed in registers and added once per chunk;
+    // the three off-diagonal contributions of an incidence hit distinct
+    // columns, so their read-modify-writes are issued together.
+    for (int lr = tid; lr < nr; lr += kThreads) {
+      int cur = s_cur[lr];
+      const int end = plan.iptr[rbeg + lr + 1];
+      const int ro = plan.racc[rbeg + lr];
+      L2 dg{0.f, 0.f};
+      int dpos = -1;
+      for (; cur < end; ++cur) {
+        const int le = plan.inc_elem[cur];
+        if (le >= cend) break;
+        const int a = plan.inc_a[cur];
+        const uint32_t pos4 = *reinterpret_cast<const uint32_t*>(plan.inc_pos + (int64_t)cur * 4);
+        const int lo = le - cbeg;
+        dpos = (pos4 >> (8 * a)) & 0xff;
+        const float2 vd = s_stage[tri4(a, a) * chunk + lo];
+        dg = l2_add(dg, L2{vd.x, vd.y});
+        int pos[3];
+        float2 v[3], acc[3];
+        int k = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          if (b == a) continue;
+          pos[k] = (pos4 >> (8 * b)) & 0xff;
+          v[k] = s_stage[tri4(a, b) * chunk + lo];
+          ++k;
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) acc[j] = s_acc[ro + pos[j]];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const L2 sum = l2_add(L2{acc[j].x, acc[j].y}, L2{v[j].x, v[j].y});
+          s_acc[ro + pos[j]] = make_float2(sum.h, sum.l);
+        }
+      }
+      if (dpos >= 0) {
+        const float2 acc = s_acc[ro + dpos];
+        const L2 sum = l2_add(L2{acc.x, acc.y}, dg);
+        s_acc[ro + dpos] = make_float2(sum.h, sum.l);
+      }
+      s_cur[lr] = cur;
+    }
+    __syncthreads();
+  }
+  // --- write the finished rows (warp per row) ---------------------------------
+  T* out = static_cast<T*>(args.out);
+  const int lane = tid & 31, warp = tid >> 5;
+  for (int lr = warp; lr < nr; lr += kThreads / 32) {
+    const int r = plan.rows[rbeg + lr];
+    const int64_t s0 = plan.indptr[r];
+    const int deg = (int)(plan.indptr[r + 1] - s0);
+    const int ro = plan.racc[rbeg + lr];
+    for (int k = lane; k < deg; k += 32) {
+      const float2 v = s_acc[ro + k];
+      out[s0 + k] = (double)v.x + (double)v.y;
+    }
+  }
+}
+
+inline size_t p1tet_smem_bytes(const tm_patch_plan& plan, int coef_kind, int chunk) {
+  size_t n2 = (size_t)plan.max_vtx * 3 + (coef_kind == TM_COEF_POINT ? plan.max_vtx : 0) + plan.max_slots +
+              (size_t)10 * chunk;
+  return n2 * sizeof(float2) + (size_t)plan.max_rows * sizeof(int) + 64;
+}
+
+inline int launch_p1tet_laplace_df64(const tm_patch_plan& plan, const tm_assemble_args& args, cudaStream_t stream) {
+  int dev = 0, max_optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  int chunk = kThreads;
+  size_t bytes = p1tet_smem_bytes(plan, args.coef_kind, chunk);
+  while (bytes > (size_t)max_optin && chunk > 32) {
+    chunk /= 2;
+    bytes = p1tet_smem_bytes(plan, args.coef_kind, chunk);
+  }
+  if (bytes > (size_t)max_optin) return TM_ERR_INDEX;
+  auto kern = p1tet_laplace_df64_kernel<double>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+    return TM_ERR_CUDA;
+  kern<<<plan.n_patches, kThreads, bytes, stream>>>(plan, args, chunk);
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+}  // namespace tmg
