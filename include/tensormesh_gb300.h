@@ -241,6 +241,24 @@ int tm_pcg_jacobi(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t
  * TM_ERR_BREAKDOWN, TM_ERR_TIMEOUT) and its iteration count / residuals. */
 int tm_pcg_result(const void* work, int32_t* iters, double* res, double* bnorm, void* stream);
 
+/*
+ * Allocation-free float32 Jacobi-PCG.  This entry point has no counterpart in
+ * the reference.  It exists for callers that cannot allocate device memory
+ * when they solve -- hosts that plan all device buffers up front, plugins
+ * whose host framework owns the only allocator, solves issued while a memory
+ * pool is exhausted.  It runs the same solver as tm_pcg_jacobi but keeps its
+ * scratch in a 32 MiB array inside this library (reserved on every GPU that
+ * loads it, until exit), so the caller passes only A, b and x.
+ * Limits and rules: n <= 1,000,000 rows, else TM_ERR_INDEX; calls share the
+ * array, so calls that overlap on the GPU race and must be serialised; the
+ * first call on a device looks up the array's address and should come before
+ * any stream capture; the call synchronises `stream` and returns the solve
+ * status (as tm_pcg_result) with the iteration count and recurrence residual.
+ */
+int tm_pcg_jacobi_noalloc(int64_t n, const int64_t* indptr, const int32_t* indices, const float* values,
+                          const float* b, float* x, double rtol, double atol, int32_t maxiter, int32_t* out_iters,
+                          double* out_res, void* stream);
+
 /* 1/diag(A) with missing diagonals taken as 1 (torch_solve.py:24-59). */
 int tm_csr_diagonal_inverse(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
                             const void* values, void* out, void* stream);

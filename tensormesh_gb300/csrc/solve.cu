@@ -598,3 +598,66 @@ extern "C" int tm_condense_rhs(int32_t dtype, int64_t n_inner, const int64_t* in
     return TM_ERR_INVALID;
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free float32 Jacobi-PCG.
+//
+// Some callers cannot allocate device memory at the moment they need a solve:
+// a host runtime that plans every device buffer up front and forbids
+// allocation afterwards (embedded / real-time deployments), a plugin that
+// receives its vectors from a host framework owning the only allocator, or a
+// solve issued while that framework's memory pool is exhausted.  For them
+// tm_pcg_jacobi_noalloc keeps the solver's scratch (state word, five vectors,
+// reduction partials) in a fixed array that lives in this library's own
+// device memory, so the caller passes only the matrix, b and x.
+//
+// The array is kTmNoAllocScratchBytes (32 MiB) on every GPU that loads the
+// library and stays reserved until the process exits.  It is shared by every
+// call: two calls whose kernels overlap on the GPU (different streams, or
+// different host threads, on one device) race on it and must be serialised
+// by the caller.  The solver state at its start is cleared on every call.
+// Limit: n <= kTmNoAllocMaxRows rows (the vectors must fit the array).
+// The first call on a device looks up the array's device address
+// (cudaGetSymbolAddress, with that device current); make that first call
+// before any stream capture.  The call synchronises its stream to read the
+// result back.
+// ---------------------------------------------------------------------------
+constexpr size_t kTmNoAllocScratchBytes = size_t(32) << 20;
+constexpr int64_t kTmNoAllocMaxRows = 1000000;
+static __device__ __align__(256) unsigned char tm_pcg_noalloc_scratch[kTmNoAllocScratchBytes];
+
+#include <mutex>
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[64] = {nullptr};
+
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TM_ERR_CUDA;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, tm_pcg_noalloc_scratch) != cudaSuccess || !p) return TM_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return TM_OK;
+}
+
+extern "C" int tm_pcg_jacobi_noalloc(int64_t n, const int64_t* indptr, const int32_t* indices, const float* values,
+                                     const float* b, float* x, double rtol, double atol, int32_t maxiter,
+                                     int32_t* out_iters, double* out_res, void* stream) {
+  if (n < 0 || maxiter < 0) return TM_ERR_INVALID;
+  if (n == 0) return TM_OK;
+  if (!indptr || !indices || !values || !b || !x) return TM_ERR_INVALID;
+  if (n > kTmNoAllocMaxRows) return TM_ERR_INDEX;
+  const int nb = tm_pcg_max_blocks(TM_F32);
+  if (nb <= 0) return TM_ERR_CUDA;
+  if (tm_pcg_workspace_bytes(TM_F32, n, 0, nb) > (int64_t)kTmNoAllocScratchBytes) return TM_ERR_INDEX;
+  void* w = nullptr;
+  int st = noalloc_scratch(&w);
+  if (st != TM_OK) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  st = launch_pcg<float>(n, indptr, indices, values, b, x, rtol, atol, maxiter, static_cast<char*>(w), nb, s);
+  if (st != TM_OK) return st;
+  return tm_pcg_result(w, out_iters, out_res, nullptr, stream);
+}
