@@ -31,8 +31,7 @@ class BackwardMaps:
     """Fixed-order reduction maps of one patch plan: the (patch, element)
     pairs of each element, and the (pair, local node) entries of each node."""
 
-    def __init__(self, topo):
-        plan = topo.plan
+    def __init__(self, topo, plan):
         dev = plan.elem.device
         E, N, B = topo.n_elements, topo.n_points, topo.n_basis
         pe = plan.elem.long()
@@ -47,11 +46,13 @@ class BackwardMaps:
         self.n_pairs = int(pe.shape[0])
 
 
-def backward_maps(topo) -> BackwardMaps:
-    m = getattr(topo, "_bw_maps", None)
-    if m is None:
-        m = topo._bw_maps = BackwardMaps(topo)
-    return m
+def backward_maps(topo, H: int = 1):
+    """(BackwardMaps, plan struct) of the plan used for H x H block slots."""
+    cache = topo.__dict__.setdefault("_bw_maps", {})
+    if H not in cache:
+        plan, struct = topo.plan_for(H)
+        cache[H] = (BackwardMaps(topo, plan), struct)
+    return cache[H]
 
 
 def segment_sum(ptr, perm, src, width):
@@ -81,7 +82,8 @@ def _args(topo, form_code, points, quadrature_order, kind, coef, scal, lame, n_c
 def run_backward(topo, form_code, points, quadrature_order, kind, coef, scal, lame, n_comp, grad_out,
                  want_points: bool, want_coef: bool):
     """Returns (grad_points [N, D] or None, grad_coef (coef's shape) or None)."""
-    maps = backward_maps(topo)
+    Hb = topo.dim if form_code == _lib.TM_FORM_ELASTICITY else 1
+    maps, plan_struct = backward_maps(topo, Hb)
     P, B, D = maps.n_pairs, topo.n_basis, topo.dim
     Q = E_.n_quadrature(topo.element_type, quadrature_order)
     dev, dtype = points.device, points.dtype
@@ -99,7 +101,7 @@ def run_backward(topo, form_code, points, quadrature_order, kind, coef, scal, la
         pair_dc = torch.empty(size, dtype=dtype, device=dev)
     bw.pair_dX = 0 if pair_dX is None else pair_dX.data_ptr()
     bw.pair_dcoef = 0 if pair_dc is None else pair_dc.data_ptr()
-    _lib.call("tm_assemble_backward", topo.plan_struct, a, bw, _lib.stream_handle(dev))
+    _lib.call("tm_assemble_backward", plan_struct, a, bw, _lib.stream_handle(dev))
     gp = gc = None
     if pair_dX is not None:
         gp = segment_sum(maps.node_ptr, maps.node_perm, pair_dX, D).view(topo.n_points, D)

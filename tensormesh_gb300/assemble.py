@@ -45,13 +45,27 @@ class MeshTopology:
         self.element_type = element_type
         self.el_id, self.dim, self.n_basis, _ = E_.element_info(element_type)
         self.elements = elements.to(torch.int32).contiguous()
+        self._elements_long = elements.long()
         self.n_points = int(points.shape[0])
         self.n_elements = int(elements.shape[0])
         self.pattern = node_pattern(elements, self.n_points)
-        self.plan = PatchPlan(elements, points.detach(), self.pattern)
-        self._plan_struct = self.plan.to_struct()
+        self._coords = points.detach()
+        self._plans = {}
+        self.plan, self._plan_struct = self.plan_for(1)
         self._block = {}
         self._incidence = None
+
+    # accumulator budget per patch in node slots: ~100 KB of shared memory at
+    # 8 bytes per value, divided by the H*H values of a block slot
+    _SLOT_BUDGET = {1: 6144, 2: 1600, 3: 700}
+
+    def plan_for(self, H: int):
+        """(PatchPlan, ctypes struct) sized for H x H block slots."""
+        budget = self._SLOT_BUDGET.get(H, max(64, 6144 // (H * H)))
+        if budget not in self._plans:
+            plan = PatchPlan(self._elements_long, self._coords, self.pattern, slot_budget=budget)
+            self._plans[budget] = (plan, plan.to_struct())
+        return self._plans[budget]
 
     def dof_pattern(self, H: int):
         if H not in self._block:
@@ -124,7 +138,8 @@ def launch_assemble(topo: MeshTopology, form_code: int, points: torch.Tensor, ou
         a.scal[i] = float(scal[i]) if i < len(scal) else 0.0
     a.lam, a.mu = float(lame[0]), float(lame[1])
     a.out = out.data_ptr()
-    plan = topo.plan_struct
+    H = n_comp if form_code == _lib.TM_FORM_LOAD else (topo.dim if form_code == _lib.TM_FORM_ELASTICITY else 1)
+    plan = topo.plan_for(1 if form_code == _lib.TM_FORM_LOAD else H)[1]
     _lib.call("tm_assemble", plan, a, _lib.stream_handle(points.device))
     return tables  # keep alive until the stream consumes it
 

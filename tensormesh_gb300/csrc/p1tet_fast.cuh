@@ -74,9 +74,43 @@ TM_D int tri4(int a, int b) {
   return i * 4 - (i * (i - 1)) / 2 + (j - i);
 }
 
-template <class T>
+// Arithmetic policies: emulated FP64 (lazy double-float, stored as float2)
+// and plain FP32 (the float32 variant of the same kernel).
+template <class A> struct Ar;
+template <> struct Ar<L2> {
+  using S = float2;
+  static TM_D L2 ld(S v) { return L2{v.x, v.y}; }
+  static TM_D S st(L2 a) { return make_float2(a.h, a.l); }
+  static TM_D L2 in(double x) { return l2_from(tm_from_double(x)); }
+  static TM_D L2 in(float x) { return L2{x, 0.f}; }
+  static TM_D L2 add(L2 a, L2 b) { return l2_add(a, b); }
+  static TM_D L2 sub(L2 a, L2 b) { return l2_sub(a, b); }
+  static TM_D L2 mul(L2 a, L2 b) { return l2_mul(a, b); }
+  static TM_D L2 neg(L2 a) { return l2_neg(a); }
+  static TM_D L2 rsqrt(L2 a) { return l2_rsqrt(a); }
+  static TM_D L2 zero() { return L2{0.f, 0.f}; }
+  static TM_D double out(S v) { return (double)v.x + (double)v.y; }
+};
+template <> struct Ar<float> {
+  using S = float;
+  static TM_D float ld(S v) { return v; }
+  static TM_D S st(float a) { return a; }
+  static TM_D float in(double x) { return (float)x; }
+  static TM_D float in(float x) { return x; }
+  static TM_D float add(float a, float b) { return a + b; }
+  static TM_D float sub(float a, float b) { return a - b; }
+  static TM_D float mul(float a, float b) { return a * b; }
+  static TM_D float neg(float a) { return -a; }
+  static TM_D float rsqrt(float a) { return rsqrtf(a); }
+  static TM_D float zero() { return 0.f; }
+  static TM_D float out(S v) { return v; }
+};
+
+template <class T, class A>
 __global__ void __launch_bounds__(kThreads)
-p1tet_laplace_df64_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
+p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
+  using P = Ar<A>;
+  using S = typename P::S;
   const int p = blockIdx.x;
   const int tid = threadIdx.x;
   const int Q = args.n_quad;
@@ -86,39 +120,34 @@ p1tet_laplace_df64_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
   if (nr == 0) return;
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float2* s_X = reinterpret_cast<float2*>(smem_raw);              // [max_vtx][3]
-  float2* s_pc = s_X + plan.max_vtx * 3;                           // [max_vtx] point coef
+  S* s_X = reinterpret_cast<S*>(smem_raw);                        // [max_vtx][3]
+  S* s_pc = s_X + plan.max_vtx * 3;                                // [max_vtx] point coef
   const int pc_len = args.coef_kind == TM_COEF_POINT ? plan.max_vtx : 0;
-  float2* s_acc = s_pc + pc_len;                                   // [max_slots]
-  float2* s_stage = s_acc + plan.max_slots;                        // [10][chunk]
+  S* s_acc = s_pc + pc_len;                                        // [max_slots]
+  S* s_stage = s_acc + plan.max_slots;                             // [10][chunk]
   int* s_cur = reinterpret_cast<int*>(s_stage + 10 * chunk);       // [max_rows] incidence cursors
 
   const T* pts = static_cast<const T*>(args.points);
   for (int i = tid; i < nv * 3; i += kThreads) {
     const int v = plan.vtx[vbeg + i / 3];
-    const df64 x = tm_from_double(pts[(int64_t)v * 3 + i % 3]);
-    s_X[i] = make_float2(x.hi, x.lo);
+    s_X[i] = P::st(P::in(pts[(int64_t)v * 3 + i % 3]));
   }
   const T* coef = static_cast<const T*>(args.coef);
   if (args.coef_kind == TM_COEF_POINT) {
-    for (int i = tid; i < nv; i += kThreads) {
-      const df64 c = tm_from_double(coef[plan.vtx[vbeg + i]]);
-      s_pc[i] = make_float2(c.hi, c.lo);
-    }
+    for (int i = tid; i < nv; i += kThreads) s_pc[i] = P::st(P::in(coef[plan.vtx[vbeg + i]]));
   }
   {
     const int lr = rbeg + nr - 1;
     const int r = plan.rows[lr];
     const int total = plan.racc[lr] + (int)(plan.indptr[r + 1] - plan.indptr[r]);
-    for (int i = tid; i < total; i += kThreads) s_acc[i] = make_float2(0.f, 0.f);
+    for (int i = tid; i < total; i += kThreads) s_acc[i] = P::st(P::zero());
   }
   for (int i = tid; i < nr; i += kThreads) s_cur[i] = plan.iptr[rbeg + i];
   // quadrature weight sum and (for point/quad coefficients) shape values
   double wsum = 0.0;
   for (int q = 0; q < Q; ++q) wsum += args.tables[q];
-  const df64 Wd = tm_from_double(wsum);
-  const L2 W{Wd.hi, Wd.lo};
-  const df64 sc = tm_from_double(args.scal[0]);
+  const A W = P::in(wsum);
+  const A sc = P::in(args.scal[0]);
   __syncthreads();
 
   // row-owner state kept across chunks: the thread's rows are tid, tid+256, ...
@@ -129,54 +158,52 @@ p1tet_laplace_df64_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
       const int pair = ebeg + le;
       const uint2 cw = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)pair * 4);
       const int lv[4] = {(int)(cw.x & 0xffff), (int)(cw.x >> 16), (int)(cw.y & 0xffff), (int)(cw.y >> 16)};
-      L2 X[4][3];
+      A X[4][3];
 #pragma unroll
       for (int b = 0; b < 4; ++b)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          const float2 v = s_X[lv[b] * 3 + d];
-          X[b][d] = L2{v.x, v.y};
-        }
-      L2 c;
+        for (int d = 0; d < 3; ++d) X[b][d] = P::ld(s_X[lv[b] * 3 + d]);
+      A c;
       if (args.coef_kind == TM_COEF_ELEMENT) {
-        c = l2_from(tm_from_double(coef[plan.elem[pair]]));
+        c = P::in(coef[plan.elem[pair]]);
       } else if (args.coef_kind == TM_COEF_POINT) {
         // sum_q w_q sum_b N_b(q) c_b / W : P1 -> weighted vertex average
         double cw_ = 0.0;
         for (int q = 0; q < Q; ++q)
-          for (int b = 0; b < 4; ++b) {
-            const float2 pc = s_pc[lv[b]];
-            cw_ += args.tables[q] * args.tables[Q + q * 4 + b] * ((double)pc.x + (double)pc.y);
-          }
-        c = l2_from(tm_from_double(cw_ / wsum));
+          for (int b = 0; b < 4; ++b) cw_ += args.tables[q] * args.tables[Q + q * 4 + b] * P::out(s_pc[lv[b]]);
+        c = P::in(cw_ / wsum);
       } else if (args.coef_kind == TM_COEF_QUAD) {
         double cw_ = 0.0;
         for (int q = 0; q < Q; ++q) cw_ += args.tables[q] * (double)coef[(int64_t)plan.elem[pair] * Q + q];
-        c = l2_from(tm_from_double(cw_ / wsum));
+        c = P::in(cw_ / wsum);
       } else {
-        c = l2_from(sc);
+        c = sc;
       }
-      L2 d[3][3];
+      A d[3][3];
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int dd = 0; dd < 3; ++dd) d[k][dd] = l2_sub(X[k + 1][dd], X[0][dd]);
-      const L2 G00 = l2_dot3(d[0], d[0]), G11 = l2_dot3(d[1], d[1]), G22 = l2_dot3(d[2], d[2]);
-      const L2 G01 = l2_dot3(d[0], d[1]), G02 = l2_dot3(d[0], d[2]), G12 = l2_dot3(d[1], d[2]);
-      const L2 A00 = l2_cof(G11, G22, G12, G12), A11 = l2_cof(G00, G22, G02, G02), A22 = l2_cof(G00, G11, G01, G01);
-      const L2 A01 = l2_cof(G02, G12, G01, G22), A02 = l2_cof(G01, G12, G02, G11), A12 = l2_cof(G01, G02, G00, G12);
-      const L2 detG = l2_add(l2_add(l2_mul(G00, A00), l2_mul(G01, A01)), l2_mul(G02, A02));
-      const L2 s = l2_mul(l2_mul(c, W), l2_rsqrt(detG));
-      const L2 k11 = l2_mul(s, A00), k22 = l2_mul(s, A11), k33 = l2_mul(s, A22);
-      const L2 k12 = l2_mul(s, A01), k13 = l2_mul(s, A02), k23 = l2_mul(s, A12);
-      const L2 k01 = l2_neg(l2_add(l2_add(k11, k12), k13));
-      const L2 k02 = l2_neg(l2_add(l2_add(k12, k22), k23));
-      const L2 k03 = l2_neg(l2_add(l2_add(k13, k23), k33));
-      const L2 k00 = l2_neg(l2_add(l2_add(k01, k02), k03));
+        for (int dd = 0; dd < 3; ++dd) d[k][dd] = P::sub(X[k + 1][dd], X[0][dd]);
+      auto dot3 = [](const A* a, const A* b) {
+        return P::add(P::add(P::mul(a[0], b[0]), P::mul(a[1], b[1])), P::mul(a[2], b[2]));
+      };
+      auto cof = [](A a, A b, A c_, A d_) { return P::sub(P::mul(a, b), P::mul(c_, d_)); };
+      const A G00 = dot3(d[0], d[0]), G11 = dot3(d[1], d[1]), G22 = dot3(d[2], d[2]);
+      const A G01 = dot3(d[0], d[1]), G02 = dot3(d[0], d[2]), G12 = dot3(d[1], d[2]);
+      const A A00 = cof(G11, G22, G12, G12), A11 = cof(G00, G22, G02, G02), A22 = cof(G00, G11, G01, G01);
+      const A A01 = cof(G02, G12, G01, G22), A02 = cof(G01, G12, G02, G11), A12 = cof(G01, G02, G00, G12);
+      const A detG = P::add(P::add(P::mul(G00, A00), P::mul(G01, A01)), P::mul(G02, A02));
+      const A s = P::mul(P::mul(c, W), P::rsqrt(detG));
+      const A k11 = P::mul(s, A00), k22 = P::mul(s, A11), k33 = P::mul(s, A22);
+      const A k12 = P::mul(s, A01), k13 = P::mul(s, A02), k23 = P::mul(s, A12);
+      const A k01 = P::neg(P::add(P::add(k11, k12), k13));
+      const A k02 = P::neg(P::add(P::add(k12, k22), k23));
+      const A k03 = P::neg(P::add(P::add(k13, k23), k33));
+      const A k00 = P::neg(P::add(P::add(k01, k02), k03));
       const int lo = le - cbeg;
-      const L2 vals[10] = {k00, k01, k02, k03, k11, k12, k13, k22, k23, k33};
+      const A vals[10] = {k00, k01, k02, k03, k11, k12, k13, k22, k23, k33};
 #pragma unroll
-      for (int u = 0; u < 10; ++u) s_stage[u * chunk + lo] = make_float2(vals[u].h, vals[u].l);
+      for (int u = 0; u < 10; ++u) s_stage[u * chunk + lo] = P::st(vals[u]);
     }
     __syncthreads();
     // --- phase B: rows gather their incidences (fixed order) -----------------
@@ -187,7 +214,7 @@ p1tet_laplace_df64_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
       int cur = s_cur[lr];
       const int end = plan.iptr[rbeg + lr + 1];
       const int ro = plan.racc[rbeg + lr];
-      L2 dg{0.f, 0.f};
+      A dg = P::zero();
       int dpos = -1;
       for (; cur < end; ++cur) {
         const int le = plan.inc_elem[cur];
@@ -196,10 +223,9 @@ p1tet_laplace_df64_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
         const uint32_t pos4 = *reinterpret_cast<const uint32_t*>(plan.inc_pos + (int64_t)cur * 4);
         const int lo = le - cbeg;
         dpos = (pos4 >> (8 * a)) & 0xff;
-        const float2 vd = s_stage[tri4(a, a) * chunk + lo];
-        dg = l2_add(dg, L2{vd.x, vd.y});
+        dg = P::add(dg, P::ld(s_stage[tri4(a, a) * chunk + lo]));
         int pos[3];
-        float2 v[3], acc[3];
+        S v[3], acc[3];
         int k = 0;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
@@ -211,16 +237,9 @@ p1tet_laplace_df64_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
 #pragma unroll
         for (int j = 0; j < 3; ++j) acc[j] = s_acc[ro + pos[j]];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          const L2 sum = l2_add(L2{acc[j].x, acc[j].y}, L2{v[j].x, v[j].y});
-          s_acc[ro + pos[j]] = make_float2(sum.h, sum.l);
-        }
+        for (int j = 0; j < 3; ++j) s_acc[ro + pos[j]] = P::st(P::add(P::ld(acc[j]), P::ld(v[j])));
       }
-      if (dpos >= 0) {
-        const float2 acc = s_acc[ro + dpos];
-        const L2 sum = l2_add(L2{acc.x, acc.y}, dg);
-        s_acc[ro + dpos] = make_float2(sum.h, sum.l);
-      }
+      if (dpos >= 0) s_acc[ro + dpos] = P::st(P::add(P::ld(s_acc[ro + dpos]), dg));
       s_cur[lr] = cur;
     }
     __syncthreads();
@@ -233,31 +252,30 @@ p1tet_laplace_df64_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
     const int64_t s0 = plan.indptr[r];
     const int deg = (int)(plan.indptr[r + 1] - s0);
     const int ro = plan.racc[rbeg + lr];
-    for (int k = lane; k < deg; k += 32) {
-      const float2 v = s_acc[ro + k];
-      out[s0 + k] = (double)v.x + (double)v.y;
-    }
+    for (int k = lane; k < deg; k += 32) out[s0 + k] = (T)P::out(s_acc[ro + k]);
   }
 }
 
-inline size_t p1tet_smem_bytes(const tm_patch_plan& plan, int coef_kind, int chunk) {
+inline size_t p1tet_smem_bytes(const tm_patch_plan& plan, int coef_kind, int chunk, size_t elem = sizeof(float2)) {
   size_t n2 = (size_t)plan.max_vtx * 3 + (coef_kind == TM_COEF_POINT ? plan.max_vtx : 0) + plan.max_slots +
               (size_t)10 * chunk;
-  return n2 * sizeof(float2) + (size_t)plan.max_rows * sizeof(int) + 64;
+  return n2 * elem + (size_t)plan.max_rows * sizeof(int) + 64;
 }
 
-inline int launch_p1tet_laplace_df64(const tm_patch_plan& plan, const tm_assemble_args& args, cudaStream_t stream) {
+template <class T, class A>
+inline int launch_p1tet_laplace_fast(const tm_patch_plan& plan, const tm_assemble_args& args, cudaStream_t stream) {
   int dev = 0, max_optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   int chunk = kThreads;
-  size_t bytes = p1tet_smem_bytes(plan, args.coef_kind, chunk);
+  const size_t es = sizeof(typename Ar<A>::S);
+  size_t bytes = p1tet_smem_bytes(plan, args.coef_kind, chunk, es);
   while (bytes > (size_t)max_optin && chunk > 32) {
     chunk /= 2;
-    bytes = p1tet_smem_bytes(plan, args.coef_kind, chunk);
+    bytes = p1tet_smem_bytes(plan, args.coef_kind, chunk, es);
   }
   if (bytes > (size_t)max_optin) return TM_ERR_INDEX;
-  auto kern = p1tet_laplace_df64_kernel<double>;
+  auto kern = p1tet_laplace_fast_kernel<T, A>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
     return TM_ERR_CUDA;
   kern<<<plan.n_patches, kThreads, bytes, stream>>>(plan, args, chunk);
