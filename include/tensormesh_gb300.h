@@ -79,6 +79,7 @@ extern "C" {
  *   inc_elem[], inc_a[]    incidence: patch-local element index, local vertex
  *   inc_pos[n_inc*B]       position of column conn[e,b] inside row conn[e,a]
  *   indptr[N+1]            node-level CSR row pointer (int64)
+ *   inc_pack[n_inc]        the same incidence packed in one word (B <= 4)
  */
 typedef struct tm_patch_plan {
   int32_t n_patches;
@@ -102,6 +103,8 @@ typedef struct tm_patch_plan {
   int32_t max_slots;  /* max node slots owned by a patch */
   int32_t max_rows;   /* max owned rows of a patch */
   int32_t max_elems;  /* max elements touching a patch */
+  const uint64_t* inc_pack; /* B <= 4: incidence record elem | a << 16 | pos4 << 24
+                               (NULL otherwise) */
 } tm_patch_plan;
 
 typedef struct tm_assemble_args {

@@ -59,9 +59,11 @@ class MeshTopology:
     # 8 bytes per value, divided by the H*H values of a block slot
     _SLOT_BUDGET = {1: 6144, 2: 1600, 3: 700}
 
-    def plan_for(self, H: int):
-        """(PatchPlan, ctypes struct) sized for H x H block slots."""
-        budget = self._SLOT_BUDGET.get(H, max(64, 6144 // (H * H)))
+    def plan_for(self, H: int, budget: int = None):
+        """(PatchPlan, ctypes struct) sized for H x H block slots (or for an
+        explicit accumulator budget in node slots)."""
+        if budget is None:
+            budget = self._SLOT_BUDGET.get(H, max(64, 6144 // (H * H)))
         if budget not in self._plans:
             plan = PatchPlan(self._elements_long, self._coords, self.pattern, slot_budget=budget)
             self._plans[budget] = (plan, plan.to_struct())
@@ -121,7 +123,8 @@ def _mesh_single_type(mesh):
 
 def launch_assemble(topo: MeshTopology, form_code: int, points: torch.Tensor, out: torch.Tensor, *,
                     quadrature_order: int, coef_kind: int = _lib.TM_COEF_SCALAR, coef=None,
-                    scal=(1.0, 0.0, 0.0), lame=(0.0, 0.0), n_comp: int = 1, precision: str = "emulated"):
+                    scal=(1.0, 0.0, 0.0), lame=(0.0, 0.0), n_comp: int = 1, precision: str = "emulated",
+                    slot_budget: int = None):
     tables = E_.kernel_tables(topo.element_type, quadrature_order, points.device)
     a = _lib.AssembleArgs()
     a.element = topo.el_id
@@ -139,7 +142,7 @@ def launch_assemble(topo: MeshTopology, form_code: int, points: torch.Tensor, ou
     a.lam, a.mu = float(lame[0]), float(lame[1])
     a.out = out.data_ptr()
     H = n_comp if form_code == _lib.TM_FORM_LOAD else (topo.dim if form_code == _lib.TM_FORM_ELASTICITY else 1)
-    plan = topo.plan_for(1 if form_code == _lib.TM_FORM_LOAD else H)[1]
+    plan = topo.plan_for(1 if form_code == _lib.TM_FORM_LOAD else H, slot_budget)[1]
     _lib.call("tm_assemble", plan, a, _lib.stream_handle(points.device))
     return tables  # keep alive until the stream consumes it
 
@@ -149,6 +152,7 @@ class ElementAssembler(nn.Module):
 
     _builtin_form: Optional[F_.BilinearForm] = None
     precision = "emulated"   # FP64 arithmetic: "emulated" (double-float) or "native"
+    slot_budget = None       # patch accumulator budget (node slots); None = default, see autotune()
 
     def __init__(self, topology: MeshTopology, points: torch.Tensor, quadrature_order: int, *args, **kwargs):
         super().__init__()
@@ -240,6 +244,40 @@ class ElementAssembler(nn.Module):
         form = self._resolve_form(func, element_data, point_data, scalar_data)
         from .autodiff import assemble_matrix
         return assemble_matrix(self, form, points, element_data, point_data, scalar_data)
+
+
+def _autotune_assembler(asm, call, dtype, budgets, reps, use_cache):
+    from . import autotune as AT
+    dev = asm.points.device
+    key = (f"assemble|{torch.cuda.get_device_name(dev)}|{asm.topology.element_type}|{type(asm).__name__}|"
+           f"{dtype}|{asm.topology.n_elements}|{asm.topology.n_points}|q{asm.quadrature_order}")
+    if use_cache:
+        hit = AT.load_cache().get(key)
+        if hit:
+            asm.slot_budget = hit["slot_budget"]
+            return hit
+
+    def run(bgt):
+        asm.slot_budget = bgt
+        call()
+    best, table = AT.pick(budgets, run, reps=reps)
+    asm.slot_budget = best
+    res = {"slot_budget": best, "table": table}
+    if use_cache:
+        AT.store_cache(key, res)
+    return res
+
+
+def _assembler_autotune(self, points=None, element_data=None, point_data=None, scalar_data=None,
+                        budgets=(512, 1024, 2048, 4096, 6144), reps: int = 3, use_cache: bool = True) -> dict:
+    """Pick the patch size (accumulator budget per patch) that assembles
+    fastest for these inputs on this GPU; the choice is cached as JSON."""
+    pts = self.points if points is None else points
+    return _autotune_assembler(self, lambda: self(pts, element_data=element_data, point_data=point_data,
+                                                  scalar_data=scalar_data), pts.dtype, budgets, reps, use_cache)
+
+
+ElementAssembler.autotune = _assembler_autotune
 
 
 class LaplaceElementAssembler(ElementAssembler):

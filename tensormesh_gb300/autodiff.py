@@ -42,7 +42,7 @@ def assemble_matrix(asm, form, points, element_data, point_data, scalar_data) ->
         from .assemble import launch_assemble
         launch_assemble(topo, _FORM_CODE[form.kind], pts, out, quadrature_order=asm.quadrature_order,
                         coef_kind=kind, coef=None if coef is None else coef.detach(), scal=(scal, 0.0, 0.0),
-                        lame=(form.lam, form.mu), precision=asm.precision)
+                        lame=(form.lam, form.mu), precision=asm.precision, slot_budget=asm.slot_budget)
         values = out
     n = topo.n_points * H
     return SparseMatrix(values, shape=(n, n), indptr=dptr, indices=dind)

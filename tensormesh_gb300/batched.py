@@ -32,33 +32,7 @@ import torch
 from . import _lib, element as E_
 from .plan import PatchPlan, node_pattern
 
-_CACHE_ENV = "TM_AUTOTUNE_CACHE"
-
-
-def _cache_path() -> str:
-    p = os.environ.get(_CACHE_ENV)
-    if p:
-        return p
-    return os.path.join(os.path.expanduser("~"), ".cache", "tensormesh_gb300", "autotune.json")
-
-
-def _load_cache() -> dict:
-    try:
-        with open(_cache_path()) as f:
-            return json.load(f)
-    except Exception:
-        return {}
-
-
-def _store_cache(key: str, value: dict):
-    data = _load_cache()
-    data[key] = value
-    path = _cache_path()
-    os.makedirs(os.path.dirname(path), exist_ok=True)
-    tmp = path + f".{os.getpid()}"
-    with open(tmp, "w") as f:
-        json.dump(data, f, indent=1, sort_keys=True)
-    os.replace(tmp, path)
+from .autotune import load_cache as _load_cache, store_cache as _store_cache
 
 
 @dataclass

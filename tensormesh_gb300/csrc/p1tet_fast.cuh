@@ -16,42 +16,6 @@
 
 namespace tmg {
 
-struct L2 {  // lazy double-float: value = h + l, |l| << |h|
-  float h, l;
-};
-
-TM_D L2 l2_from(df64 a) { return {a.hi, a.lo}; }
-TM_D L2 l2_sub(L2 a, L2 b) {
-  const float s = __fsub_rn(a.h, b.h);
-  const float bb = __fsub_rn(s, a.h);
-  const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(-b.h, bb));
-  return {s, __fadd_rn(e, __fsub_rn(a.l, b.l))};
-}
-TM_D L2 l2_add(L2 a, L2 b) {
-  const float s = __fadd_rn(a.h, b.h);
-  const float bb = __fsub_rn(s, a.h);
-  const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
-  return {s, __fadd_rn(e, __fadd_rn(a.l, b.l))};
-}
-TM_D L2 l2_mul(L2 a, L2 b) {
-  const float p = __fmul_rn(a.h, b.h);
-  float e = __fmaf_rn(a.h, b.h, -p);
-  e = __fmaf_rn(a.h, b.l, e);
-  e = __fmaf_rn(a.l, b.h, e);
-  return {p, e};
-}
-TM_D L2 l2_neg(L2 a) { return {-a.h, -a.l}; }
-TM_D L2 l2_norm(L2 a) {
-  const float s = __fadd_rn(a.h, a.l);
-  return {s, __fsub_rn(a.l, __fsub_rn(s, a.h))};
-}
-// dot of two 3-vectors
-TM_D L2 l2_dot3(const L2* a, const L2* b) {
-  return l2_add(l2_add(l2_mul(a[0], b[0]), l2_mul(a[1], b[1])), l2_mul(a[2], b[2]));
-}
-// a*b - c*d
-TM_D L2 l2_cof(L2 a, L2 b, L2 c, L2 d) { return l2_sub(l2_mul(a, b), l2_mul(c, d)); }
-
 // 1/sqrt(x) for x > 0: MUFU estimate, one Newton step in double-float
 // (y1 = y0 + y0 (1 - x y0^2) / 2; the residual 1 - x y0^2 is formed with
 // error-free products so the step doubles the ~22 correct bits).
@@ -216,11 +180,15 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
       const int ro = plan.racc[rbeg + lr];
       A dg = P::zero();
       int dpos = -1;
-      for (; cur < end; ++cur) {
-        const int le = plan.inc_elem[cur];
+      // one packed record per incidence, the next one loaded ahead (the
+      // sentinel's element field 0xffff is >= every chunk end)
+      uint64_t rec = cur < end ? plan.inc_pack[cur] : ~0ull;
+      for (;;) {
+        const int le = (int)(rec & 0xffff);
         if (le >= cend) break;
-        const int a = plan.inc_a[cur];
-        const uint32_t pos4 = *reinterpret_cast<const uint32_t*>(plan.inc_pos + (int64_t)cur * 4);
+        const uint64_t next = (cur + 1 < end) ? plan.inc_pack[cur + 1] : ~0ull;
+        const int a = (int)((rec >> 16) & 0xff);
+        const uint32_t pos4 = (uint32_t)(rec >> 24);
         const int lo = le - cbeg;
         dpos = (pos4 >> (8 * a)) & 0xff;
         dg = P::add(dg, P::ld(s_stage[tri4(a, a) * chunk + lo]));
@@ -238,6 +206,8 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
         for (int j = 0; j < 3; ++j) acc[j] = s_acc[ro + pos[j]];
 #pragma unroll
         for (int j = 0; j < 3; ++j) s_acc[ro + pos[j]] = P::st(P::add(P::ld(acc[j]), P::ld(v[j])));
+        rec = next;
+        ++cur;
       }
       if (dpos >= 0) s_acc[ro + dpos] = P::st(P::add(P::ld(s_acc[ro + dpos]), dg));
       s_cur[lr] = cur;

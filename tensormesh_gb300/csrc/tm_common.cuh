@@ -129,3 +129,44 @@ struct Strided {
   int s;
   TM_D R& operator[](int i) const { return p[i * s]; }
 };
+
+// Lazy double-float: value = h + l with |l| << |h| but not renormalised after
+// every operation (error-free products by FMA; TwoSum only where two leading
+// parts are added).  Used on the hot paths where full df64 normalisation
+// would double the instruction count.
+struct L2 {
+  float h, l;
+};
+
+TM_D L2 l2_from(df64 a) { return {a.hi, a.lo}; }
+TM_D L2 l2_sub(L2 a, L2 b) {
+  const float s = __fsub_rn(a.h, b.h);
+  const float bb = __fsub_rn(s, a.h);
+  const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(-b.h, bb));
+  return {s, __fadd_rn(e, __fsub_rn(a.l, b.l))};
+}
+TM_D L2 l2_add(L2 a, L2 b) {
+  const float s = __fadd_rn(a.h, b.h);
+  const float bb = __fsub_rn(s, a.h);
+  const float e = __fadd_rn(__fsub_rn(a.h, __fsub_rn(s, bb)), __fsub_rn(b.h, bb));
+  return {s, __fadd_rn(e, __fadd_rn(a.l, b.l))};
+}
+TM_D L2 l2_mul(L2 a, L2 b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return {p, e};
+}
+TM_D L2 l2_neg(L2 a) { return {-a.h, -a.l}; }
+TM_D L2 l2_norm(L2 a) {
+  const float s = __fadd_rn(a.h, a.l);
+  return {s, __fsub_rn(a.l, __fsub_rn(s, a.h))};
+}
+// dot of two 3-vectors
+TM_D L2 l2_dot3(const L2* a, const L2* b) {
+  return l2_add(l2_add(l2_mul(a[0], b[0]), l2_mul(a[1], b[1])), l2_mul(a[2], b[2]));
+}
+// a*b - c*d
+TM_D L2 l2_cof(L2 a, L2 b, L2 c, L2 d) { return l2_sub(l2_mul(a, b), l2_mul(c, d)); }
+

@@ -252,6 +252,16 @@ class PatchPlan:
         self.inc_elem = inc_local_elem.to(i32).to(torch.int16).contiguous()
         self.inc_a = a.to(torch.uint8).contiguous()
         self.inc_pos = inc_pos.to(torch.uint8).contiguous()
+        # P1 elements (B <= 4): one 64-bit record per incidence = local element
+        # (bits 0-15) | local vertex a (16-23) | positions of columns 0..3
+        # (24-55, 8 bits each), so the row owner issues one load per incidence
+        if B <= 4:
+            pk = inc_local_elem.long() | (a.long() << 16)
+            for bb in range(B):
+                pk = pk | (inc_pos[:, bb].long() << (24 + 8 * bb))
+            self.inc_pack = pk.contiguous()
+        else:
+            self.inc_pack = None
         self.indptr = indptr.contiguous()
         self.max_vtx = int(verts_per_part.max()) if E else 0
         self.max_slots = int(slots_per_part.max()) if N else 0
@@ -273,6 +283,7 @@ class PatchPlan:
         for name in ("vptr", "vtx", "eptr", "elem", "econn", "rptr", "rows", "racc", "iptr",
                      "inc_elem", "inc_a", "inc_pos", "indptr"):
             setattr(s, name, getattr(self, name).data_ptr())
+        s.inc_pack = 0 if self.inc_pack is None else self.inc_pack.data_ptr()
         s.max_vtx, s.max_slots, s.max_rows, s.max_elems = self.max_vtx, self.max_slots, self.max_rows, self.max_elems
         return s
 
