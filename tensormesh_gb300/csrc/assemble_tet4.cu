@@ -6,9 +6,9 @@
 
 namespace tmg {
 int assemble_tet4(const tm_patch_plan& plan, const tm_assemble_args& a, cudaStream_t s) {
-  if (plan.inc_pack && a.form == TM_FORM_LAPLACE && a.dtype == TM_F64 && a.precision == TM_PREC_EMULATED)
+  if (p1tet_fast_ok(plan) && a.form == TM_FORM_LAPLACE && a.dtype == TM_F64 && a.precision == TM_PREC_EMULATED)
     return launch_p1tet_laplace_fast<double, L2>(plan, a, s);
-  if (plan.inc_pack && a.form == TM_FORM_LAPLACE && a.dtype == TM_F32)
+  if (p1tet_fast_ok(plan) && a.form == TM_FORM_LAPLACE && a.dtype == TM_F32)
     return launch_p1tet_laplace_fast<float, float>(plan, a, s);
   return assemble_element<TM_TET4>(plan, a, s);
 }

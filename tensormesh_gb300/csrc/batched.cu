@@ -50,8 +50,8 @@ struct BatchArgs {
   int32_t chunk;
 };
 
-constexpr int kBatchThreads = 256;
-constexpr int kBatchGroup = 4;  // lanes per CSR row (P1 triangles: 7 entries per row)
+constexpr int kBatchThreads = 512;
+constexpr int kRowIlp = 8;  // CSR entries fetched together per row (P1 triangles: 7 per interior row)
 
 __device__ __forceinline__ double cta_sum(double v, double* red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -64,6 +64,29 @@ __device__ __forceinline__ double cta_sum(double v, double* red) {
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
   __syncthreads();
   return t;  // thread 0
+}
+
+// two sums with one pair of barriers; results valid in thread 0
+__device__ __forceinline__ void cta_sum2(double& a, double& b, double (*red)[2]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  if (lane == 0) {
+    red[warp][0] = a;
+    red[warp][1] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    a = b = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += red[w][0];
+      b += red[w][1];
+    }
+  }
+  __syncthreads();
 }
 
 // combine one partial per CTA of the cluster, in rank order (same value everywhere)
@@ -81,6 +104,7 @@ __global__ void __launch_bounds__(kBatchThreads) batched_assemble_pcg_kernel(Bat
   const unsigned C = cl.num_blocks();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[32];
+  __shared__ double red2[32][2];
   __shared__ double part[2][3];  // [parity][pq, rz, rr]
   __shared__ int task;
 
@@ -112,8 +136,6 @@ __global__ void __launch_bounds__(kBatchThreads) batched_assemble_pcg_kernel(Bat
     const int64_t r0 = rb + min(n, (int64_t)rank * per), r1 = rb + min(n, (int64_t)(rank + 1) * per);
     const float* val = static_cast<const float*>(A.mat.out);
     const float* b = static_cast<const float*>(A.load.out);
-    const int g = threadIdx.x / kBatchGroup, lane = threadIdx.x % kBatchGroup;
-    const int ngroups = kBatchThreads / kBatchGroup;
     double rz_l = 0, rr_l = 0, bb_l = 0;
     for (int64_t row = r0 + threadIdx.x; row < r1; row += kBatchThreads) {
       const bool fixed = A.dirichlet[row] != 0;
@@ -158,25 +180,29 @@ __global__ void __launch_bounds__(kBatchThreads) batched_assemble_pcg_kernel(Bat
       }
       if (it == A.maxiter) break;
       double pq_l = 0;
-      // uniform trip count across the CTA: every lane reaches each shuffle
-      for (int64_t base = r0; base < r1; base += ngroups) {
-        const int64_t row = base + g;
-        const bool valid = row < r1;
+      // one thread per row; each row's entries are fetched kRowIlp at a time
+      // (all loads of a chunk issued before the first use), so a warp keeps
+      // 32 x kRowIlp independent gathers in flight instead of one chain
+      for (int64_t row = r0 + threadIdx.x; row < r1; row += kBatchThreads) {
+        const int64_t k0 = A.indptr[row], k1 = A.indptr[row + 1];
         float s = 0.f;
-        if (valid)
-          for (int64_t kk = A.indptr[row] + lane; kk < A.indptr[row + 1]; kk += kBatchGroup) {
-            const int c = A.indices[kk];
-            s += val[kk] * (A.z[c] + beta * pold[c]);
+        for (int64_t kb = k0; kb < k1; kb += kRowIlp) {
+          int c[kRowIlp];
+          float v[kRowIlp];
+#pragma unroll
+          for (int j = 0; j < kRowIlp; ++j) {
+            const bool ok = kb + j < k1;
+            c[j] = ok ? A.indices[kb + j] : (int)row;
+            v[j] = ok ? val[kb + j] : 0.f;
           }
 #pragma unroll
-        for (int o = kBatchGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kBatchGroup);
-        if (valid && lane == 0) {
-          const bool fixed = A.dirichlet[row] != 0;
-          const float pv = A.z[row] + beta * pold[row];
-          const float qv = fixed ? 0.f : s;
-          A.q[row] = qv;
-          pq_l += (double)pv * qv;
+          for (int j = 0; j < kRowIlp; ++j) s += v[j] * (A.z[c[j]] + beta * pold[c[j]]);
         }
+        const bool fixed = A.dirichlet[row] != 0;
+        const float pv = A.z[row] + beta * pold[row];
+        const float qv = fixed ? 0.f : s;
+        A.q[row] = qv;
+        pq_l += (double)pv * qv;
       }
       t0 = cta_sum(pq_l, red);
       if (threadIdx.x == 0) part[par][0] = t0;
@@ -200,11 +226,10 @@ __global__ void __launch_bounds__(kBatchThreads) batched_assemble_pcg_kernel(Bat
         rz_n += (double)rv * zv;
         rr_n += (double)rv * rv;
       }
-      t0 = cta_sum(rz_n, red);
-      t1 = cta_sum(rr_n, red);
+      cta_sum2(rz_n, rr_n, red2);
       if (threadIdx.x == 0) {
-        part[par][1] = t0;
-        part[par][2] = t1;
+        part[par][1] = rz_n;
+        part[par][2] = rr_n;
       }
       __threadfence();
       cl.sync();

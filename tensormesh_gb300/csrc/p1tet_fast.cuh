@@ -84,13 +84,32 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
   if (nr == 0) return;
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  S* s_X = reinterpret_cast<S*>(smem_raw);                        // [max_vtx][3]
+  int64_t* s_out0 = reinterpret_cast<int64_t*>(smem_raw);         // [kThreads] CSR offset of each row
+  uint32_t* s_rd = reinterpret_cast<uint32_t*>(s_out0 + kThreads); // [kThreads] acc offset | degree << 24
+  S* s_X = reinterpret_cast<S*>(s_rd + kThreads);                  // [max_vtx][3]
   S* s_pc = s_X + plan.max_vtx * 3;                                // [max_vtx] point coef
   const int pc_len = args.coef_kind == TM_COEF_POINT ? plan.max_vtx : 0;
   S* s_acc = s_pc + pc_len;                                        // [max_slots]
   S* s_stage = s_acc + plan.max_slots;                             // [10][chunk]
-  int* s_cur = reinterpret_cast<int*>(s_stage + 10 * chunk);       // [max_rows] incidence cursors
 
+  // ---- phase 0: row state (the launcher guarantees nr <= kThreads, so a
+  // thread owns at most one row; its incidence cursor and the next packed
+  // record stay in registers across chunks), coordinates, coefficients
+  const bool owner = tid < nr;
+  int cur = 0, end = 0, ro = 0;
+  uint64_t rec = ~0ull;
+  if (owner) {
+    const int r = plan.rows[rbeg + tid];
+    const int64_t o0 = plan.indptr[r];
+    const int deg = (int)(plan.indptr[r + 1] - o0);
+    ro = plan.racc[rbeg + tid];
+    cur = plan.iptr[rbeg + tid];
+    end = plan.iptr[rbeg + tid + 1];
+    if (cur < end) rec = plan.inc_pack[cur];
+    s_out0[tid] = o0;
+    s_rd[tid] = (uint32_t)ro | ((uint32_t)deg << 24);
+    for (int k = 0; k < deg; ++k) s_acc[ro + k] = P::st(P::zero());
+  }
   const T* pts = static_cast<const T*>(args.points);
   for (int i = tid; i < nv * 3; i += kThreads) {
     const int v = plan.vtx[vbeg + i / 3];
@@ -100,27 +119,34 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
   if (args.coef_kind == TM_COEF_POINT) {
     for (int i = tid; i < nv; i += kThreads) s_pc[i] = P::st(P::in(coef[plan.vtx[vbeg + i]]));
   }
-  {
-    const int lr = rbeg + nr - 1;
-    const int r = plan.rows[lr];
-    const int total = plan.racc[lr] + (int)(plan.indptr[r + 1] - plan.indptr[r]);
-    for (int i = tid; i < total; i += kThreads) s_acc[i] = P::st(P::zero());
-  }
-  for (int i = tid; i < nr; i += kThreads) s_cur[i] = plan.iptr[rbeg + i];
-  // quadrature weight sum and (for point/quad coefficients) shape values
   double wsum = 0.0;
   for (int q = 0; q < Q; ++q) wsum += args.tables[q];
   const A W = P::in(wsum);
   const A sc = P::in(args.scal[0]);
+  const bool per_elem = args.coef_kind == TM_COEF_ELEMENT;
+  // element data of this thread's next element (threads tid < chunk handle
+  // element cbeg + tid of every chunk), loaded one chunk ahead
+  const bool worker = tid < chunk;
+  uint2 cw_next = make_uint2(0u, 0u);
+  T c_next = T(0);
+  if (worker && tid < ne) {
+    cw_next = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)(ebeg + tid) * 4);
+    if (per_elem) c_next = coef[plan.elem[ebeg + tid]];
+  }
   __syncthreads();
 
-  // row-owner state kept across chunks: the thread's rows are tid, tid+256, ...
   for (int cbeg = 0; cbeg < ne; cbeg += chunk) {
     const int cend = min(ne, cbeg + chunk);
     // --- phase A -------------------------------------------------------------
-    for (int le = cbeg + tid; le < cend; le += kThreads) {
+    const int le = cbeg + tid;
+    if (worker && le < cend) {
       const int pair = ebeg + le;
-      const uint2 cw = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)pair * 4);
+      const uint2 cw = cw_next;
+      const T c_raw = c_next;
+      if (le + chunk < ne) {
+        cw_next = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)(pair + chunk) * 4);
+        if (per_elem) c_next = coef[plan.elem[pair + chunk]];
+      }
       const int lv[4] = {(int)(cw.x & 0xffff), (int)(cw.x >> 16), (int)(cw.y & 0xffff), (int)(cw.y >> 16)};
       A X[4][3];
 #pragma unroll
@@ -128,8 +154,8 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
 #pragma unroll
         for (int d = 0; d < 3; ++d) X[b][d] = P::ld(s_X[lv[b] * 3 + d]);
       A c;
-      if (args.coef_kind == TM_COEF_ELEMENT) {
-        c = P::in(coef[plan.elem[pair]]);
+      if (per_elem) {
+        c = P::in(c_raw);
       } else if (args.coef_kind == TM_COEF_POINT) {
         // sum_q w_q sum_b N_b(q) c_b / W : P1 -> weighted vertex average
         double cw_ = 0.0;
@@ -170,26 +196,21 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
       for (int u = 0; u < 10; ++u) s_stage[u * chunk + lo] = P::st(vals[u]);
     }
     __syncthreads();
-    // --- phase B: rows gather their incidences (fixed order) -----------------
-    // The diagonal of the row is summed in registers and added once per chunk;
+    // --- phase B: the row owner adds its incidences of this chunk (fixed
+    // order).  The diagonal is summed in registers and added once per chunk;
     // the three off-diagonal contributions of an incidence hit distinct
-    // columns, so their read-modify-writes are issued together.
-    for (int lr = tid; lr < nr; lr += kThreads) {
-      int cur = s_cur[lr];
-      const int end = plan.iptr[rbeg + lr + 1];
-      const int ro = plan.racc[rbeg + lr];
+    // columns, so their read-modify-writes are issued together.  The record
+    // that ends the loop is the first one of the next chunk.
+    if (owner) {
       A dg = P::zero();
       int dpos = -1;
-      // one packed record per incidence, the next one loaded ahead (the
-      // sentinel's element field 0xffff is >= every chunk end)
-      uint64_t rec = cur < end ? plan.inc_pack[cur] : ~0ull;
       for (;;) {
-        const int le = (int)(rec & 0xffff);
-        if (le >= cend) break;
+        const int lel = (int)(rec & 0xffff);
+        if (lel >= cend) break;  // also the sentinel (0xffff >= every chunk end)
         const uint64_t next = (cur + 1 < end) ? plan.inc_pack[cur + 1] : ~0ull;
         const int a = (int)((rec >> 16) & 0xff);
         const uint32_t pos4 = (uint32_t)(rec >> 24);
-        const int lo = le - cbeg;
+        const int lo = lel - cbeg;
         dpos = (pos4 >> (8 * a)) & 0xff;
         dg = P::add(dg, P::ld(s_stage[tri4(a, a) * chunk + lo]));
         int pos[3];
@@ -210,26 +231,31 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
         ++cur;
       }
       if (dpos >= 0) s_acc[ro + dpos] = P::st(P::add(P::ld(s_acc[ro + dpos]), dg));
-      s_cur[lr] = cur;
     }
     __syncthreads();
   }
-  // --- write the finished rows (warp per row) ---------------------------------
+  // --- write the finished rows: half a warp per row, row metadata from shared
   T* out = static_cast<T*>(args.out);
-  const int lane = tid & 31, warp = tid >> 5;
-  for (int lr = warp; lr < nr; lr += kThreads / 32) {
-    const int r = plan.rows[rbeg + lr];
-    const int64_t s0 = plan.indptr[r];
-    const int deg = (int)(plan.indptr[r + 1] - s0);
-    const int ro = plan.racc[rbeg + lr];
-    for (int k = lane; k < deg; k += 32) out[s0 + k] = (T)P::out(s_acc[ro + k]);
+  const int hl = tid & 15;
+  for (int lr = tid >> 4; lr < nr; lr += kThreads / 16) {
+    const int64_t o0 = s_out0[lr];
+    const uint32_t rd = s_rd[lr];
+    const int r0 = (int)(rd & 0xffffffu), deg = (int)(rd >> 24);
+    for (int k = hl; k < deg; k += 16) out[o0 + k] = (T)P::out(s_acc[r0 + k]);
   }
 }
 
 inline size_t p1tet_smem_bytes(const tm_patch_plan& plan, int coef_kind, int chunk, size_t elem = sizeof(float2)) {
   size_t n2 = (size_t)plan.max_vtx * 3 + (coef_kind == TM_COEF_POINT ? plan.max_vtx : 0) + plan.max_slots +
               (size_t)10 * chunk;
-  return n2 * elem + (size_t)plan.max_rows * sizeof(int) + 64;
+  return (size_t)kThreads * (sizeof(int64_t) + sizeof(uint32_t)) + n2 * elem + 64;
+}
+
+// The fast path needs every patch to own at most kThreads rows (one row per
+// thread) and fewer than 2^24 accumulator slots; other plans take the generic
+// patch kernel.
+inline bool p1tet_fast_ok(const tm_patch_plan& plan) {
+  return plan.inc_pack != nullptr && plan.max_rows <= kThreads && plan.max_slots < (1 << 24);
 }
 
 template <class T, class A>

@@ -82,23 +82,31 @@ def block_pattern(indptr: torch.Tensor, indices: torch.Tensor, H: int):
     return dptr, out
 
 
-def rcb_partition(coords: torch.Tensor, n_levels: int) -> torch.Tensor:
-    """Recursive coordinate bisection: split every segment at its median
-    along its longest extent, ``n_levels`` times.  Returns the part id of
-    each point (parts numbered in RCB leaf order, spatially coherent)."""
+def rcb_partition(coords: torch.Tensor, n_levels: int = None, n_parts: int = None) -> torch.Tensor:
+    """Recursive coordinate bisection into ``n_parts`` parts (default
+    ``2**n_levels``).  A segment that must become k parts is cut along its
+    longest extent at the point count k_left / k of its points, where
+    k_left = k // 2, and the two sides go on to become k_left and k - k_left
+    parts; so parts hold floor or ceil of N / n_parts points whatever
+    n_parts is.  Returns the part id of each point (parts numbered in RCB
+    leaf order, spatially coherent)."""
     N = coords.shape[0]
     dev = coords.device
+    if n_parts is None:
+        n_parts = 1 << int(n_levels or 0)
+    n_parts = max(1, int(n_parts))
     c = coords.to(torch.float64)
     D = c.shape[1]
     perm = torch.arange(N, device=dev)
-    seg = torch.zeros(N, dtype=torch.int64, device=dev)
+    seg = torch.zeros(N, dtype=torch.int64, device=dev)        # first part id of the point's segment
+    kpart = torch.zeros(n_parts, dtype=torch.int64, device=dev)  # parts still to make, at first-part ids
+    kpart[0] = n_parts
     ar = torch.arange(N, device=dev)
-    for level in range(n_levels):
-        nseg = 1 << level
+    while N and int(kpart.max()) > 1:
         cp = c[perm]
         idx = seg.unsqueeze(1).expand(N, D)
-        mx = torch.full((nseg, D), -math.inf, dtype=torch.float64, device=dev).scatter_reduce(0, idx, cp, "amax")
-        mn = torch.full((nseg, D), math.inf, dtype=torch.float64, device=dev).scatter_reduce(0, idx, cp, "amin")
+        mx = torch.full((n_parts, D), -math.inf, dtype=torch.float64, device=dev).scatter_reduce(0, idx, cp, "amax")
+        mn = torch.full((n_parts, D), math.inf, dtype=torch.float64, device=dev).scatter_reduce(0, idx, cp, "amin")
         axis = torch.argmax(mx - mn, dim=1)
         val = cp[ar, axis[seg]]
         o1 = torch.argsort(val, stable=True)
@@ -106,10 +114,17 @@ def rcb_partition(coords: torch.Tensor, n_levels: int) -> torch.Tensor:
         order = o1[o2]
         perm = perm[order]
         seg = seg[order]
-        counts = torch.bincount(seg, minlength=nseg)
+        counts = torch.bincount(seg, minlength=n_parts)
         start = torch.cumsum(counts, 0) - counts
         pos = ar - start[seg]
-        seg = 2 * seg + (pos >= (counts[seg] + 1) // 2).long()
+        k = kpart[seg]
+        kl = k // 2
+        cut = (counts[seg] * kl) // torch.clamp(k, min=1)
+        seg = seg + ((k > 1) & (pos >= cut)).long() * kl
+        firsts = torch.nonzero(kpart > 1, as_tuple=True)[0]
+        kk = kpart[firsts]
+        kpart[firsts + kk // 2] = kk - kk // 2
+        kpart[firsts] = kk // 2
     part = torch.empty(N, dtype=torch.int64, device=dev)
     part[perm] = seg
     return part
@@ -156,7 +171,7 @@ class PatchPlan:
     """Device arrays of the patch structure plus the ctypes view of them."""
 
     def __init__(self, elements: torch.Tensor, coords: torch.Tensor, pattern: NodePattern,
-                 slot_budget: int = 6144, max_rows_cap: int = 2048, groups: torch.Tensor = None):
+                 slot_budget: int = 6144, max_rows_cap: int = 256, groups: torch.Tensor = None):
         dev = elements.device
         E, B = elements.shape
         N = pattern.n_points
@@ -177,16 +192,15 @@ class PatchPlan:
         else:
             avg_deg = float(deg.float().mean()) if N else 1.0
             target_rows = max(16, min(max_rows_cap, int(slot_budget / max(avg_deg, 1.0))))
-            n_levels = max(0, math.ceil(math.log2(max(1, N) / target_rows)))
+            n_parts = max(1, math.ceil(N / target_rows))
             while True:
-                part = rcb_partition(coords, n_levels) if N else torch.zeros(0, dtype=torch.int64, device=dev)
-                n_parts = 1 << n_levels
+                part = rcb_partition(coords, n_parts=n_parts) if N else torch.zeros(0, dtype=torch.int64, device=dev)
                 slots_per_part = torch.zeros(n_parts, dtype=torch.int64, device=dev).index_add_(0, part, deg)
                 rows_per_part = torch.bincount(part, minlength=n_parts)
                 if N == 0 or (int(slots_per_part.max()) <= 2 * slot_budget and
                               int(rows_per_part.max()) <= max_rows_cap):
                     break
-                n_levels += 1
+                n_parts = n_parts + max(1, n_parts // 32)
             self.part = part
         self.n_patches = n_parts
 
