@@ -71,7 +71,7 @@ extern "C" {
  * All arrays are device arrays.
  *
  *   vptr[P+1], vtx[]       local vertex table of each patch (global node ids)
- *   eptr[P+1], elem[]      elements touching each patch (global ids, sorted)
+ *   eptr[P+1], elem[]      elements touching each patch (global ids)
  *   econn[eptr[P]*B]       element connectivity in patch-local vertex ids
  *   rptr[P+1], rows[]      owned rows of each patch (global node ids)
  *   racc[]                 accumulator offset (in node slots) of each owned row
@@ -79,7 +79,18 @@ extern "C" {
  *   inc_elem[], inc_a[]    incidence: patch-local element index, local vertex
  *   inc_pos[n_inc*B]       position of column conn[e,b] inside row conn[e,a]
  *   indptr[N+1]            node-level CSR row pointer (int64)
- *   inc_pack[n_inc]        the same incidence packed in one word (B <= 4)
+ *   inc_pack[n_inc]        P1 tetrahedra: the incidence in one 64-bit record
+ *   inc_pack32[n_inc]      the same in 32 bits, when it fits
+ *   rdiag[n_rows]          position of each owned row's own column (rows[] order)
+ *
+ * Records (o_j = (a + 1 + j) mod 4, pos o_j = position of column conn[e, o_j]
+ * inside row conn[e, a]):
+ *   inc_pack:   local element (bits 0-15) | a (16-17) | pos o_0, o_1, o_2
+ *               (8 bits each, from bit 18)
+ *   inc_pack32: local element (bits 0-14) | a (15-16) | pos o_0, o_1, o_2
+ *               (5 bits each, from bit 17); built when every row has at most
+ *               32 entries and every patch at most 32767 elements
+ * Elements inside a patch are in processing order (not sorted by id).
  */
 typedef struct tm_patch_plan {
   int32_t n_patches;
@@ -103,8 +114,9 @@ typedef struct tm_patch_plan {
   int32_t max_slots;  /* max node slots owned by a patch */
   int32_t max_rows;   /* max owned rows of a patch */
   int32_t max_elems;  /* max elements touching a patch */
-  const uint64_t* inc_pack; /* B <= 4: incidence record elem | a << 16 | pos4 << 24
-                               (NULL otherwise) */
+  const uint64_t* inc_pack;   /* P1 tetrahedra (NULL otherwise) */
+  const uint32_t* inc_pack32; /* NULL when it does not fit */
+  const uint8_t* rdiag;       /* with inc_pack */
 } tm_patch_plan;
 
 typedef struct tm_assemble_args {

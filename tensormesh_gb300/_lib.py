@@ -51,7 +51,7 @@ class PatchPlan(ctypes.Structure):
         ("inc_elem", P), ("inc_a", P), ("inc_pos", P), ("indptr", P),
         ("max_vtx", ctypes.c_int32), ("max_slots", ctypes.c_int32),
         ("max_rows", ctypes.c_int32), ("max_elems", ctypes.c_int32),
-        ("inc_pack", P),
+        ("inc_pack", P), ("inc_pack32", P), ("rdiag", P),
     ]
 
 

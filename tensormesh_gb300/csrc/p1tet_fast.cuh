@@ -38,6 +38,29 @@ TM_D int tri4(int a, int b) {
   return i * 4 - (i * (i - 1)) / 2 + (j - i);
 }
 
+// Incidence records (see tm_patch_plan): local element, local vertex a and the
+// row positions of the off-diagonal columns o_j = (a + 1 + j) mod 4.
+template <class W> struct Rec;
+template <> struct Rec<uint64_t> {
+  static constexpr uint64_t kEnd = ~0ull;  // local element 0xffff: past every chunk
+  static TM_D int elem(uint64_t r) { return (int)(r & 0xffff); }
+  static TM_D int a(uint64_t r) { return (int)((r >> 16) & 3); }
+  static TM_D int pos(uint64_t r, int j) { return (int)((r >> (18 + 8 * j)) & 0xff); }
+  static TM_D const uint64_t* ptr(const tm_patch_plan& p) { return p.inc_pack; }
+};
+template <> struct Rec<uint32_t> {
+  static constexpr uint32_t kEnd = ~0u;    // local element 0x7fff: past every chunk
+  static TM_D int elem(uint32_t r) { return (int)(r & 0x7fff); }
+  static TM_D int a(uint32_t r) { return (int)((r >> 15) & 3); }
+  static TM_D int pos(uint32_t r, int j) { return (int)((r >> (17 + 5 * j)) & 31); }
+  static TM_D const uint32_t* ptr(const tm_patch_plan& p) { return p.inc_pack32; }
+};
+
+// Staged unique-entry index (tri4 order) of the diagonal (nibble 0) and of the
+// off-diagonal entries (a, o_j) (nibbles 1-3), 16 bits per local vertex a:
+//   a=0: 0 1 2 3   a=1: 4 5 6 1   a=2: 7 8 2 5   a=3: 9 3 6 8
+constexpr uint64_t kTet4Stage = 0x8639528716543210ull;
+
 // Arithmetic policies: emulated FP64 (lazy double-float, stored as float2)
 // and plain FP32 (the float32 variant of the same kernel).
 template <class A> struct Ar;
@@ -70,10 +93,12 @@ template <> struct Ar<float> {
   static TM_D float out(S v) { return v; }
 };
 
-template <class T, class A>
+template <class T, class A, class RW>
 __global__ void __launch_bounds__(kThreads)
 p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
   using P = Ar<A>;
+  using R = Rec<RW>;
+  const RW* recs = R::ptr(plan);
   using S = typename P::S;
   const int p = blockIdx.x;
   const int tid = threadIdx.x;
@@ -96,16 +121,17 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
   // thread owns at most one row; its incidence cursor and the next packed
   // record stay in registers across chunks), coordinates, coefficients
   const bool owner = tid < nr;
-  int cur = 0, end = 0, ro = 0;
-  uint64_t rec = ~0ull;
+  int cur = 0, end = 0, ro = 0, dpos = 0;
+  RW rec = R::kEnd;
   if (owner) {
     const int r = plan.rows[rbeg + tid];
     const int64_t o0 = plan.indptr[r];
     const int deg = (int)(plan.indptr[r + 1] - o0);
     ro = plan.racc[rbeg + tid];
+    dpos = plan.rdiag[rbeg + tid];
     cur = plan.iptr[rbeg + tid];
     end = plan.iptr[rbeg + tid + 1];
-    if (cur < end) rec = plan.inc_pack[cur];
+    if (cur < end) rec = recs[cur];
     s_out0[tid] = o0;
     s_rd[tid] = (uint32_t)ro | ((uint32_t)deg << 24);
     for (int k = 0; k < deg; ++k) s_acc[ro + k] = P::st(P::zero());
@@ -203,34 +229,31 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
     // that ends the loop is the first one of the next chunk.
     if (owner) {
       A dg = P::zero();
-      int dpos = -1;
+      bool any = false;
       for (;;) {
-        const int lel = (int)(rec & 0xffff);
-        if (lel >= cend) break;  // also the sentinel (0xffff >= every chunk end)
-        const uint64_t next = (cur + 1 < end) ? plan.inc_pack[cur + 1] : ~0ull;
-        const int a = (int)((rec >> 16) & 0xff);
-        const uint32_t pos4 = (uint32_t)(rec >> 24);
+        const int lel = R::elem(rec);
+        if (lel >= cend) break;  // also the end record (its element field is past every chunk)
+        const RW next = (cur + 1 < end) ? recs[cur + 1] : R::kEnd;
+        const int a = R::a(rec);
         const int lo = lel - cbeg;
-        dpos = (pos4 >> (8 * a)) & 0xff;
-        dg = P::add(dg, P::ld(s_stage[tri4(a, a) * chunk + lo]));
+        const uint32_t u = (uint32_t)(kTet4Stage >> (16 * a));
+        dg = P::add(dg, P::ld(s_stage[(int)(u & 15u) * chunk + lo]));
         int pos[3];
         S v[3], acc[3];
-        int k = 0;
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          if (b == a) continue;
-          pos[k] = (pos4 >> (8 * b)) & 0xff;
-          v[k] = s_stage[tri4(a, b) * chunk + lo];
-          ++k;
+        for (int j = 0; j < 3; ++j) {
+          pos[j] = ro + R::pos(rec, j);
+          v[j] = s_stage[(int)((u >> (4 * j + 4)) & 15u) * chunk + lo];
         }
 #pragma unroll
-        for (int j = 0; j < 3; ++j) acc[j] = s_acc[ro + pos[j]];
+        for (int j = 0; j < 3; ++j) acc[j] = s_acc[pos[j]];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) s_acc[ro + pos[j]] = P::st(P::add(P::ld(acc[j]), P::ld(v[j])));
+        for (int j = 0; j < 3; ++j) s_acc[pos[j]] = P::st(P::add(P::ld(acc[j]), P::ld(v[j])));
+        any = true;
         rec = next;
         ++cur;
       }
-      if (dpos >= 0) s_acc[ro + dpos] = P::st(P::add(P::ld(s_acc[ro + dpos]), dg));
+      if (any) s_acc[ro + dpos] = P::st(P::add(P::ld(s_acc[ro + dpos]), dg));
     }
     __syncthreads();
   }
@@ -255,11 +278,12 @@ inline size_t p1tet_smem_bytes(const tm_patch_plan& plan, int coef_kind, int chu
 // thread) and fewer than 2^24 accumulator slots; other plans take the generic
 // patch kernel.
 inline bool p1tet_fast_ok(const tm_patch_plan& plan) {
-  return plan.inc_pack != nullptr && plan.max_rows <= kThreads && plan.max_slots < (1 << 24);
+  return plan.inc_pack != nullptr && plan.rdiag != nullptr && plan.max_rows <= kThreads &&
+         plan.max_slots < (1 << 24);
 }
 
-template <class T, class A>
-inline int launch_p1tet_laplace_fast(const tm_patch_plan& plan, const tm_assemble_args& args, cudaStream_t stream) {
+template <class T, class A, class RW>
+inline int launch_p1tet_kernel(const tm_patch_plan& plan, const tm_assemble_args& args, cudaStream_t stream) {
   int dev = 0, max_optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -271,11 +295,17 @@ inline int launch_p1tet_laplace_fast(const tm_patch_plan& plan, const tm_assembl
     bytes = p1tet_smem_bytes(plan, args.coef_kind, chunk, es);
   }
   if (bytes > (size_t)max_optin) return TM_ERR_INDEX;
-  auto kern = p1tet_laplace_fast_kernel<T, A>;
+  auto kern = p1tet_laplace_fast_kernel<T, A, RW>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
     return TM_ERR_CUDA;
   kern<<<plan.n_patches, kThreads, bytes, stream>>>(plan, args, chunk);
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+template <class T, class A>
+inline int launch_p1tet_laplace_fast(const tm_patch_plan& plan, const tm_assemble_args& args, cudaStream_t stream) {
+  if (plan.inc_pack32) return launch_p1tet_kernel<T, A, uint32_t>(plan, args, stream);
+  return launch_p1tet_kernel<T, A, uint64_t>(plan, args, stream);
 }
 
 }  // namespace tmg

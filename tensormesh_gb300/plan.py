@@ -26,6 +26,10 @@ import torch
 from . import _lib
 
 
+# elements staged per chunk by the patch kernels (their block size)
+PATCH_CHUNK = 256
+
+
 @dataclass
 class NodePattern:
     n_points: int
@@ -226,6 +230,16 @@ class PatchPlan:
         eptr[1:] = torch.cumsum(elems_per_part, 0)
         if E and int(elems_per_part.max()) > 65535:
             raise NotImplementedError("patch with more than 65535 elements")
+        # processing order inside a patch: the kernels stage PATCH_CHUNK
+        # elements at a time, and a row's incidences come in runs of
+        # neighbouring element ids; dealing the sorted elements out over the
+        # m = ceil(n / PATCH_CHUNK) chunks (element k goes to chunk k mod m)
+        # gives every row a similar number of incidences in every chunk
+        if E:
+            rank = torch.arange(pairs.shape[0], device=dev) - eptr[pair_patch]
+            m = torch.clamp((elems_per_part[pair_patch] + PATCH_CHUNK - 1) // PATCH_CHUNK, min=1)
+            deal = torch.argsort(pair_patch * (1 << 32) + (rank % m) * (1 << 16) + rank // m)
+            pair_patch, pair_elem = pair_patch[deal], pair_elem[deal]
 
         # -- patch-local vertex tables
         pconn = el[pair_elem]                                           # [n_pairs, B]
@@ -266,16 +280,35 @@ class PatchPlan:
         self.inc_elem = inc_local_elem.to(i32).to(torch.int16).contiguous()
         self.inc_a = a.to(torch.uint8).contiguous()
         self.inc_pos = inc_pos.to(torch.uint8).contiguous()
-        # P1 elements (B <= 4): one 64-bit record per incidence = local element
-        # (bits 0-15) | local vertex a (16-23) | positions of columns 0..3
-        # (24-55, 8 bits each), so the row owner issues one load per incidence
-        if B <= 4:
+        # P1 tetrahedra: one record per incidence, so the row owner issues one
+        # load per incidence.  With o_j = (a + 1 + j) mod 4 the record holds the
+        # positions of the three off-diagonal columns conn[e, o_j] in the row:
+        #   64-bit: local element (bits 0-15) | a (16-17) | pos o_0, o_1, o_2
+        #           (8 bits each from bit 18);
+        #   32-bit (rows of at most 32 entries, at most 32767 elements per
+        #           patch): local element (0-14) | a (15-16) | pos o_0, o_1,
+        #           o_2 (5 bits each from bit 17).
+        # rdiag holds the position of each owned row's own column (rows order).
+        self.inc_pack = self.inc_pack32 = self.rdiag = None
+        if B == 4:
+            others = (a.unsqueeze(1) + 1 + torch.arange(3, device=dev)) % 4          # [n_inc, 3]
+            po = torch.gather(inc_pos, 1, others).long()                             # [n_inc, 3]
             pk = inc_local_elem.long() | (a.long() << 16)
-            for bb in range(B):
-                pk = pk | (inc_pos[:, bb].long() << (24 + 8 * bb))
+            for j in range(3):
+                pk = pk | (po[:, j] << (18 + 8 * j))
             self.inc_pack = pk.contiguous()
-        else:
-            self.inc_pack = None
+            n_inc = int(a.shape[0])
+            dpos_inc = inc_pos[torch.arange(n_inc, device=dev), a.long()].long()
+            has = inc_per_row > 0
+            first = torch.clamp(iptr[:-1], max=max(0, n_inc - 1))
+            rdiag = torch.where(has, dpos_inc[first] if n_inc else torch.zeros_like(first), torch.zeros_like(first))
+            self.rdiag = rdiag.to(torch.uint8).contiguous()
+            max_deg = int(deg.max()) if N else 0
+            if max_deg <= 32 and (not E or int(elems_per_part.max()) <= 32767):
+                pk32 = inc_local_elem.long() | (a.long() << 15)
+                for j in range(3):
+                    pk32 = pk32 | (po[:, j] << (17 + 5 * j))
+                self.inc_pack32 = pk32.to(torch.int64).to(torch.int32).contiguous()  # uint32 bit pattern
         self.indptr = indptr.contiguous()
         self.max_vtx = int(verts_per_part.max()) if E else 0
         self.max_slots = int(slots_per_part.max()) if N else 0
@@ -298,6 +331,8 @@ class PatchPlan:
                      "inc_elem", "inc_a", "inc_pos", "indptr"):
             setattr(s, name, getattr(self, name).data_ptr())
         s.inc_pack = 0 if self.inc_pack is None else self.inc_pack.data_ptr()
+        s.inc_pack32 = 0 if self.inc_pack32 is None else self.inc_pack32.data_ptr()
+        s.rdiag = 0 if self.rdiag is None else self.rdiag.data_ptr()
         s.max_vtx, s.max_slots, s.max_rows, s.max_elems = self.max_vtx, self.max_slots, self.max_rows, self.max_elems
         return s
 

@@ -106,3 +106,44 @@ def test_patch_plan_replay_reproduces_oracle(etype, budget):
     ip, ix, dv = fem.assemble_csr(pts, el.numpy(), etype, "laplace", 2)
     got = replay_plan(plan, Ke, ix.shape[0])
     assert np.max(np.abs(got - dv)) <= 1e-13 * np.max(np.abs(dv))
+
+
+def replay_packed(plan: PatchPlan, Ke: np.ndarray, nnz: int, bits32: bool) -> np.ndarray:
+    """numpy replay of the P1-tet kernel's phase B from the packed records
+    (inc_pack / inc_pack32 and rdiag), in the kernel's chunked order."""
+    out = np.full(nnz, np.nan)
+    rec = (plan.inc_pack32.numpy().astype(np.int64) & 0xFFFFFFFF) if bits32 else plan.inc_pack.numpy()
+    emask, ash, psh, pw = (0x7FFF, 15, 17, 5) if bits32 else (0xFFFF, 16, 18, 8)
+    rptr, rows, racc = plan.rptr.numpy(), plan.rows.numpy(), plan.racc.numpy()
+    eptr, elem, iptr = plan.eptr.numpy(), plan.elem.numpy(), plan.iptr.numpy()
+    rdiag, indptr = plan.rdiag.numpy(), plan.indptr.numpy()
+    for p in range(plan.n_patches):
+        for lr in range(rptr[p], rptr[p + 1]):
+            r = rows[lr]
+            acc = np.zeros(indptr[r + 1] - indptr[r])
+            for k in range(iptr[lr], iptr[lr + 1]):
+                w = int(rec[k])
+                le, a = w & emask, (w >> ash) & 3
+                e = elem[eptr[p] + le]
+                acc[rdiag[lr]] += Ke[e, a, a]
+                for j in range(3):
+                    b = (a + 1 + j) % 4
+                    acc[(w >> (psh + pw * j)) & ((1 << pw) - 1)] += Ke[e, a, b]
+            out[indptr[r]:indptr[r + 1]] = acc
+    return out
+
+
+@pytest.mark.parametrize("budget", [64, 300, 100000])
+def test_packed_tet_records_reproduce_oracle(budget):
+    m = _meshes()["tetra"]
+    el = m.cells["tetra"]
+    pts = m.points.numpy()
+    p = node_pattern(el, m.n_points)
+    plan = PatchPlan(el, m.points, p, slot_budget=budget)
+    assert plan.inc_pack is not None and plan.inc_pack32 is not None and plan.rdiag is not None
+    assert plan.max_rows <= 256
+    Ke = fem.element_matrices(pts, el.numpy(), "tetra", "laplace", 2)
+    ip, ix, dv = fem.assemble_csr(pts, el.numpy(), "tetra", "laplace", 2)
+    for bits32 in (False, True):
+        got = replay_packed(plan, Ke, ix.shape[0], bits32)
+        assert np.max(np.abs(got - dv)) <= 1e-13 * np.max(np.abs(dv))
