@@ -76,7 +76,7 @@ template <> struct Ar<L2> {
   static TM_D L2 neg(L2 a) { return l2_neg(a); }
   static TM_D L2 rsqrt(L2 a) { return l2_rsqrt(a); }
   static TM_D L2 zero() { return L2{0.f, 0.f}; }
-  static TM_D double out(S v) { return (double)v.x + (double)v.y; }
+  static TM_D double out(S v) { return tm_to_double(df64{v.x, v.y}); }
 };
 template <> struct Ar<float> {
   using S = float;
@@ -94,7 +94,7 @@ template <> struct Ar<float> {
 };
 
 template <class T, class A, class RW>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
 p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
   using P = Ar<A>;
   using R = Rec<RW>;
@@ -260,10 +260,12 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
   // --- write the finished rows: half a warp per row, row metadata from shared
   T* out = static_cast<T*>(args.out);
   const int hl = tid & 15;
+#pragma unroll 1
   for (int lr = tid >> 4; lr < nr; lr += kThreads / 16) {
     const int64_t o0 = s_out0[lr];
     const uint32_t rd = s_rd[lr];
     const int r0 = (int)(rd & 0xffffffu), deg = (int)(rd >> 24);
+#pragma unroll 1
     for (int k = hl; k < deg; k += 16) out[o0 + k] = (T)P::out(s_acc[r0 + k]);
   }
 }
