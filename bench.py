@@ -376,24 +376,31 @@ def run_ours(args):
             from tensormesh_gb300.learned import LearnedPreconditioner
             from tensormesh_gb300.train_learned import load_weights
             coords = mesh.points[~mesh.boundary_mask].contiguous()
-            pre = LearnedPreconditioner(load_weights(wpath, dev), coarse_target=512)
-            torch.cuda.synchronize()
-            t0s = time.perf_counter()
-            pre.setup(K_ii, coords)
-            torch.cuda.synchronize()
-            t_setup = time.perf_counter() - t0s
-            x = torch.zeros_like(f_i)
-            pre.solve(K_ii, f_i, x.clone(), rtol=1e-8, coords=coords, maxiter=2000)  # warm
-            torch.cuda.synchronize()
-            t0s = time.perf_counter()
-            linfo = pre.solve(K_ii, f_i, x, rtol=1e-8, coords=coords, maxiter=2000)
-            torch.cuda.synchronize()
-            t_solve = time.perf_counter() - t0s
-            pcg.update({"learned_seconds_to_1e-8": t_solve, "learned_setup_seconds": t_setup,
-                        "learned_iterations": linfo.iterations, "learned_true_residual": linfo.residual,
-                        "learned_status": linfo.status, "learned_fallback": linfo.fallback,
-                        "learned_vs_jacobi_time_ratio": (t_solve + t_setup) / (tb - ta),
-                        "learned_vs_jacobi_time_ratio_solve_only": t_solve / (tb - ta)})
+            model = load_weights(wpath, dev)
+            two = {}
+            for name, use in (("learned", True), ("unit_weights", False)):
+                pre = LearnedPreconditioner(model, coarse_target=512, use_network=use)
+                pre.solve(K_ii, f_i, torch.zeros_like(f_i), rtol=1e-8, coords=coords, maxiter=3000)  # warm-up
+                pre._setup_key = None
+                torch.cuda.synchronize()
+                t0s = time.perf_counter()
+                pre.setup(K_ii, coords)
+                torch.cuda.synchronize()
+                t_setup = time.perf_counter() - t0s
+                x = torch.zeros_like(f_i)
+                linfo = pre.solve(K_ii, f_i, x, rtol=1e-8, coords=coords, maxiter=3000)
+                torch.cuda.synchronize()
+                t_solve = time.perf_counter() - t0s - t_setup
+                two[name] = {"seconds_to_1e-8": t_setup + t_solve, "setup_seconds": t_setup,
+                             "solve_seconds": t_solve, "iterations": linfo.iterations,
+                             "true_residual": linfo.residual, "status": linfo.status, "fallback": linfo.fallback,
+                             "vs_jacobi_time_ratio": (t_setup + t_solve) / (tb - ta)}
+            L = two["learned"]
+            pcg.update({"learned_seconds_to_1e-8": L["seconds_to_1e-8"], "learned_setup_seconds": L["setup_seconds"],
+                        "learned_iterations": L["iterations"], "learned_true_residual": L["true_residual"],
+                        "learned_status": L["status"], "learned_fallback": L["fallback"],
+                        "learned_vs_jacobi_time_ratio": L["vs_jacobi_time_ratio"],
+                        "two_level_unit_weights": two["unit_weights"]})
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -230,9 +230,39 @@ int tm_quadrature_points(int32_t element, int32_t dtype, int32_t n_quad, const d
                          const void* points, const int32_t* elements, int64_t n_elements,
                          void* out, void* stream);
 
+/*
+ * Two-level preconditioner of the learned solver (no counterpart in the
+ * reference, whose K.solve has only Jacobi): z = C r + (I - C K) S (I - K C) r
+ * with C = P K_c^-1 P^T (P piecewise constant over nc aggregates) and
+ * S = diag(sw).  float32 inside; r and z are FP64 device vectors of length n.
+ * work: float32 scratch of 2 n + 4 nc values.  Graph-capturable (no host
+ * synchronisation, no allocation).
+ */
+typedef struct tm_twolevel {
+  int64_t n;                  /* fine dofs */
+  int32_t nc;                 /* aggregates */
+  int32_t pad0;
+  const int32_t* agg;         /* [n] aggregate of each dof */
+  const int64_t* agg_ptr;     /* [nc+1] dof range of each aggregate in agg_perm */
+  const int32_t* agg_perm;    /* [n] dofs grouped by aggregate */
+  const float* kc_inv;        /* [nc*nc] K_c^-1, row-major */
+  const int64_t* kp_indptr;   /* [n+1] K P as CSR with nc columns */
+  const int32_t* kp_indices;
+  const float* kp_values;
+  int64_t k_nnz;              /* K (float32 values) */
+  const int64_t* k_indptr;
+  const int32_t* k_indices;
+  const float* k_values;
+  const float* sw;            /* [n] smoother weights w_i / K_ii */
+  float* work;
+} tm_twolevel;
+
+int tm_twolevel_apply(const tm_twolevel* t, const double* r, double* z, void* stream);
+
 /* y = A x for CSR A (replaces SparseMatrix @ / spmv, sparse/mm/__init__.py:
- * 22-72).  dtype applies to values, x and y. */
-int tm_spmv_csr(int32_t dtype, int64_t n_rows, const int64_t* indptr, const int32_t* indices,
+ * 22-72).  dtype applies to values, x and y; nnz = indptr[n_rows] (it sets
+ * the lanes per row; the row extents come from indptr). */
+int tm_spmv_csr(int32_t dtype, int64_t n_rows, int64_t nnz, const int64_t* indptr, const int32_t* indices,
                 const void* values, const void* x, void* y, void* stream);
 
 /*

@@ -36,7 +36,7 @@ EXPORTS = [
     "tm_batched_assemble_pcg", "tm_batched_max_clusters", "tm_patch_smem_bytes",
     "tm_mpnn_input_fwd", "tm_mpnn_layer_fwd", "tm_mpnn_readout_fwd", "tm_mpnn_readout_bwd",
     "tm_mpnn_layer_bwd", "tm_mpnn_input_bwd", "tm_gather_axpy_f32",
-    "tm_pcg_jacobi_noalloc",
+    "tm_pcg_jacobi_noalloc", "tm_twolevel_apply",
 ]
 
 P = ctypes.c_void_p
@@ -52,6 +52,16 @@ class PatchPlan(ctypes.Structure):
         ("max_vtx", ctypes.c_int32), ("max_slots", ctypes.c_int32),
         ("max_rows", ctypes.c_int32), ("max_elems", ctypes.c_int32),
         ("inc_pack", P), ("inc_pack32", P), ("rdiag", P),
+    ]
+
+
+class TwoLevel(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int64), ("nc", ctypes.c_int32), ("pad0", ctypes.c_int32),
+        ("agg", P), ("agg_ptr", P), ("agg_perm", P), ("kc_inv", P),
+        ("kp_indptr", P), ("kp_indices", P), ("kp_values", P),
+        ("k_nnz", ctypes.c_int64), ("k_indptr", P), ("k_indices", P), ("k_values", P),
+        ("sw", P), ("work", P),
     ]
 
 
@@ -99,7 +109,7 @@ def _declare(lib):
     sig = {
         "tm_assemble": [ctypes.POINTER(PatchPlan), ctypes.POINTER(AssembleArgs), P],
         "tm_quadrature_points": [i32, i32, i32, P, P, P, i64, P, P],
-        "tm_spmv_csr": [i32, i64, P, P, P, P, P, P],
+        "tm_spmv_csr": [i32, i64, i64, P, P, P, P, P, P],
         "tm_pcg_jacobi": [i32, i64, P, P, P, P, P, ctypes.c_double, ctypes.c_double, i32, P, i64, P],
         "tm_pcg_result": [P, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_double),
                           ctypes.POINTER(ctypes.c_double), P],
@@ -121,6 +131,7 @@ def _declare(lib):
         "tm_gather_axpy_f32": [i64, P, P, P, P, P, P, P, P],
         "tm_pcg_jacobi_noalloc": [i64, P, P, P, P, P, ctypes.c_double, ctypes.c_double, i32,
                                   ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_double), P],
+        "tm_twolevel_apply": [ctypes.POINTER(TwoLevel), P, P, P],
     }
     lib.tm_patch_smem_bytes.argtypes = [i32, i32, i32, i32, ctypes.POINTER(PatchPlan), i32, i32]
     lib.tm_patch_smem_bytes.restype = i64

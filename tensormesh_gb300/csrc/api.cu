@@ -1,6 +1,7 @@
 // C-ABI entry points: argument validation and dispatch.
 #include <cstdio>
 #include "tm_common.cuh"
+#include "spmv.cuh"
 #include "../../include/tensormesh_gb300.h"
 
 namespace tmg {
@@ -56,22 +57,6 @@ __global__ void quad_points_kernel(int Q, const double* __restrict__ tables, con
   for (int d = 0; d < D; ++d) out[i * D + d] = (T)acc[d];
 }
 
-// CSR SpMV: a group of G lanes per row, FP accumulation in the value type.
-template <class T, int G>
-__global__ void spmv_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ idx,
-                            const T* __restrict__ val, const T* __restrict__ x, T* __restrict__ y) {
-  int64_t gid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int64_t row = gid / G;
-  int lane = threadIdx.x % G;
-  T s = 0;
-  if (row < n) {
-    int64_t b = indptr[row], e = indptr[row + 1];
-    for (int64_t k = b + lane; k < e; k += G) s += val[k] * x[idx[k]];
-  }
-#pragma unroll
-  for (int off = G / 2; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off, G);
-  if (row < n && lane == 0) y[row] = s;
-}
 }  // namespace tmg
 
 extern "C" int tm_assemble(const tm_patch_plan* plan, const tm_assemble_args* args, void* stream) {
@@ -179,22 +164,17 @@ extern "C" int tm_quadrature_points(int32_t element, int32_t dtype, int32_t n_qu
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
 
-extern "C" int tm_spmv_csr(int32_t dtype, int64_t n_rows, const int64_t* indptr, const int32_t* indices,
+extern "C" int tm_spmv_csr(int32_t dtype, int64_t n_rows, int64_t nnz, const int64_t* indptr, const int32_t* indices,
                            const void* values, const void* x, void* y, void* stream) {
-  if (n_rows < 0) return TM_ERR_INVALID;
+  if (n_rows < 0 || nnz < 0) return TM_ERR_INVALID;
   if (n_rows == 0) return TM_OK;
-  if (!indptr || !indices || !values || !x || !y) return TM_ERR_INVALID;
+  if (!indptr || (nnz > 0 && (!indices || !values)) || !x || !y) return TM_ERR_INVALID;
+  if (dtype != TM_F64 && dtype != TM_F32) return TM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  constexpr int G = 8;
-  int64_t threads = n_rows * G;
-  int grid = (int)((threads + 255) / 256);
+  // nnz only picks the lanes per row; the rows' extents come from indptr
   if (dtype == TM_F64)
-    tmg::spmv_kernel<double, G><<<grid, 256, 0, s>>>(n_rows, indptr, indices, (const double*)values,
-                                                   (const double*)x, (double*)y);
-  else if (dtype == TM_F32)
-    tmg::spmv_kernel<float, G><<<grid, 256, 0, s>>>(n_rows, indptr, indices, (const float*)values,
-                                                  (const float*)x, (float*)y);
+    tmg::launch_spmv<double>(n_rows, nnz, indptr, indices, (const double*)values, (const double*)x, (double*)y, s);
   else
-    return TM_ERR_INVALID;
+    tmg::launch_spmv<float>(n_rows, nnz, indptr, indices, (const float*)values, (const float*)x, (float*)y, s);
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }

@@ -1,27 +1,28 @@
-"""Learned preconditioner: a mesh-graph message-passing network (MPNN) used
-inside flexible PCG, with Jacobi-PCG as fallback and judge.
+"""Learned preconditioner: a mesh-graph message-passing network (MPNN) sets
+the smoother of a two-level preconditioner used inside flexible PCG, with
+Jacobi-PCG as fallback and judge.
 
-Architecture (hidden width 64, BF16 weights and activations on the tensor
-cores, FP32 accumulation -- kernels in csrc/mpnn.cu):
+Network (hidden width 64, BF16 weights and activations on the tensor cores,
+FP32 accumulation -- kernels in csrc/mpnn.cu):
   * graph = the condensed stiffness K_ii; edge weights a_ij =
     K_ij / sqrt(K_ii K_jj) (off-diagonal, symmetric);
-  * input  x = D^-1/2 r / s, s = ||D^-1/2 r|| / sqrt(n)  (scale-equivariant);
+  * input: the feature 1 on every node, so the lift sees the row sums of A;
   * 4 message-passing layers: a lift H0 = relu(x w0 + (A x) w1 + b0) and
     three hidden layers H = relu(H W_s + (A H) W_n + b);
-  * a message-passing readout y = H wr0 + A (H wr1); the correction is
-    z = s D^-1/2 y.
+  * a message-passing readout y = H wr0 + A (H wr1).
 
-The network is the smoother of a two-level preconditioner: a coarse
-correction on node aggregates (piecewise-constant prolongation P over an
-RCB partition of the dofs, K_c = P^T K P inverted once) removes the smooth
-error a local network cannot see, then the MPNN corrects the rest:
-    z_c = P K_c^-1 P^T r ;  z = z_c + MPNN(r - K z_c) ;  z += P K_c^-1 P^T (r - K z).
-It is trained on residual/error pairs (r_k, e_k) of the plain Jacobi-PCG
-iterates x_k of method-generated systems, minimising the energy norm
-||z(r_k) - e_k||_K^2 / ||e_k||_K^2, with the hand-written forward and
-backward kernels and Adam.  Flexible CG (Polak-Ribiere beta) tolerates the
-nonlinear preconditioner; the true FP64 residual ||b - K x|| / ||b|| from
-the plain SpMV decides convergence, and a stagnating solve falls back to
+Preconditioner: coarse correction C = P K_c^-1 P^T on node aggregates
+(piecewise-constant P over Morton-curve parts of the dofs, K_c = P^T K P
+inverted once) and the damped Jacobi smoother S = diag(w) D^-1 with
+w = 1/2 + sigmoid(y):
+    z = C r + (I - C K) S (I - K C) r.
+The network runs once per matrix, at set-up; an iteration costs two SpMVs
+(K and the thin K P), two coarse solves and vector updates, all on the device
+without host synchronisation.  Training minimises the energy norm
+||z(r_k) - e_k||_K^2 / ||e_k||_K^2 over residual/error pairs taken from the
+preconditioner's own flexible-PCG iterates on generated systems, with the
+hand-written forward and backward kernels and Adam.  The true FP64 residual
+||b - K x|| / ||b|| decides convergence, and a stagnating solve falls back to
 Jacobi-PCG.
 """
 from __future__ import annotations
@@ -34,7 +35,7 @@ from typing import Dict, List, Optional
 import torch
 
 from . import _lib
-from .plan import rcb_partition_grouped
+from .plan import morton_parts
 from .solve import SolveInfo, pcg_jacobi_raw, spmv_raw, true_relative_residual
 
 F = 64
@@ -57,6 +58,7 @@ class Graph:
             (rows[rows == indices.long()],), values.double()[rows == indices.long()])
         diag = torch.where(diag > 0, diag, torch.ones_like(diag))
         self.dinv_sqrt = (1.0 / diag.sqrt()).float().contiguous()
+        self.dinv = (1.0 / diag).contiguous()                          # FP64
         a = values.double() * (1.0 / diag.sqrt())[rows] * (1.0 / diag.sqrt())[indices.long()]
         a = torch.where(rows == indices.long(), torch.zeros_like(a), a)
         self.aoff = a.float().contiguous()
@@ -166,40 +168,73 @@ class MPNN:
 
 
 class CoarseSpace:
-    """Piecewise-constant aggregation of the dofs into RCB parts; K_c =
-    P^T K P is formed once (deterministic segmented sums) and inverted once."""
+    """Piecewise-constant aggregation of the dofs into parts of about
+    ``target`` dofs, consecutive along a Morton curve of their coordinates.  Stores P (the aggregate of each dof), K P as a CSR
+    (n x n_c, a few entries per row: only rows next to an aggregate border
+    have more than one), and K_c^-1 = (P^T K P)^-1, inverted once after a
+    symmetric diagonal scaling (Cholesky in float32, in FP64 if float32 is not
+    positive definite) and kept in float32 for the matvec; the preconditioner
+    only needs it approximately."""
 
     def __init__(self, indptr, indices, values, coords, target: int = 512):
+        from .adjoint import segment_sum
         dev = values.device
         n = indptr.shape[0] - 1
-        deg = torch.ones(n, dtype=torch.int64, device=dev)
-        agg = rcb_partition_grouped(coords, torch.zeros(n, dtype=torch.int64, device=dev), deg, float(target), target)
+        agg = morton_parts(coords, target)
         self.agg = agg
         nc = int(agg.max()) + 1
         self.nc = nc
         rows = torch.repeat_interleave(torch.arange(n, device=dev), indptr[1:] - indptr[:-1])
-        key = agg[rows] * nc + agg[indices.long()]
+        # K P: entry (i, c) = sum of K_ij over j in aggregate c
+        key = rows * nc + agg[indices.long()]
         order = torch.argsort(key, stable=True)
-        k_sorted = key[order]
-        uniq, counts = torch.unique_consecutive(k_sorted, return_counts=True)
+        uniq, counts = torch.unique_consecutive(key[order], return_counts=True)
         ptr = torch.zeros(uniq.shape[0] + 1, dtype=torch.int64, device=dev)
         ptr[1:] = torch.cumsum(counts, 0)
-        from .adjoint import segment_sum
-        vals = segment_sum(ptr, order.contiguous(), values.double().contiguous(), 1)
+        kp_vals = segment_sum(ptr, order.contiguous(), values.double().contiguous(), 1)
+        kp_rows = torch.div(uniq, nc, rounding_mode="floor")
+        self.kp_indices = (uniq - kp_rows * nc).to(torch.int32).contiguous()
+        self.kp_indptr = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+        self.kp_indptr[1:] = torch.cumsum(torch.bincount(kp_rows, minlength=n), 0)
+        self.kp_values = kp_vals.contiguous()
+        # K_c = P^T (K P): sum the rows of K P by aggregate
+        key2 = agg[kp_rows] * nc + self.kp_indices.long()
+        order2 = torch.argsort(key2, stable=True)
+        uniq2, counts2 = torch.unique_consecutive(key2[order2], return_counts=True)
+        ptr2 = torch.zeros(uniq2.shape[0] + 1, dtype=torch.int64, device=dev)
+        ptr2[1:] = torch.cumsum(counts2, 0)
+        kc_vals = segment_sum(ptr2, order2.contiguous(), kp_vals, 1)
         Kc = torch.zeros(nc * nc, dtype=torch.float64, device=dev)
-        Kc[uniq] = vals
+        Kc[uniq2] = kc_vals
         Kc = Kc.view(nc, nc)
-        self.Kc_inv = torch.linalg.inv(Kc).contiguous()
+        s = 1.0 / torch.sqrt(torch.clamp(torch.diagonal(Kc), min=torch.finfo(torch.float64).tiny))
+        Ks = Kc * s[:, None] * s[None, :]                  # unit diagonal
+        L, info = torch.linalg.cholesky_ex(Ks.float())
+        if int(info) == 0:
+            Kinv = torch.cholesky_inverse(L).double()
+        else:                                             # float32 not enough: factor in FP64
+            Kinv = torch.cholesky_inverse(torch.linalg.cholesky(Ks))
+        self.Kc_inv = (Kinv * s[:, None] * s[None, :]).float().contiguous()
         self.agg_order = torch.argsort(agg, stable=True)
         self.agg_ptr = torch.zeros(nc + 1, dtype=torch.int64, device=dev)
         self.agg_ptr[1:] = torch.cumsum(torch.bincount(agg, minlength=nc), 0)
+        self.agg32 = agg.to(torch.int32).contiguous()
+        self.agg_order32 = self.agg_order.to(torch.int32).contiguous()
+        self.kp_values32 = self.kp_values.float().contiguous()
+
+    def restrict_solve(self, r: torch.Tensor) -> torch.Tensor:
+        """y_c = K_c^-1 P^T r (coarse values, FP64)."""
+        from .adjoint import segment_sum
+        rc = segment_sum(self.agg_ptr, self.agg_order, r.double().contiguous(), 1)
+        return (self.Kc_inv @ rc.float()).double()
 
     def apply(self, r: torch.Tensor) -> torch.Tensor:
         """P K_c^-1 P^T r."""
-        from .adjoint import segment_sum
-        rc = segment_sum(self.agg_ptr, self.agg_order, r.double().contiguous(), 1)
-        zc = self.Kc_inv @ rc
-        return zc[self.agg].to(r.dtype)
+        return self.restrict_solve(r)[self.agg].to(r.dtype)
+
+    def kp(self, yc: torch.Tensor) -> torch.Tensor:
+        """K P y_c."""
+        return spmv_raw(self.kp_indptr, self.kp_indices, self.kp_values, yc.double().contiguous())
 
 
 @dataclass
@@ -210,7 +245,17 @@ class LearnedSolveInfo(SolveInfo):
 
 
 class LearnedPreconditioner:
-    """Two-level preconditioner with an MPNN smoother, for flexible PCG."""
+    """Two-level preconditioner whose smoother weights come from the MPNN.
+
+    At set-up the network reads the normalised operator (edge weights a_ij,
+    input feature 1 on every node, so its first layer sees the row sums of A)
+    and returns one value y_i per dof; the smoother is the damped Jacobi step
+    S = diag(w) D^-1 with w_i = 1/2 + sigmoid(y_i) in (1/2, 3/2) (w = 1 when
+    the network outputs 0).  With the coarse correction C = P K_c^-1 P^T the
+    preconditioner is
+        z = C r + (I - C K) S (I - K C) r,
+    symmetric positive definite, applied with one SpMV by K and one by the
+    thin K P.  ``use_network=False`` gives the same method with w = 1."""
 
     def __init__(self, model: Optional[MPNN] = None, device="cuda", coarse_target: int = 512,
                  use_network: bool = True):
@@ -220,101 +265,172 @@ class LearnedPreconditioner:
         self._setup_key = None
 
     def setup(self, A, coords):
-        key = (A.values.data_ptr(), A.values._version, A.nnz)
+        key = (A.values.data_ptr(), A.values._version, A.nnz, self.use_network)
         if key == self._setup_key:
             return
         self.A = A
         self.G = Graph(A.indptr, A.indices, A.values.detach())
         self.coarse = CoarseSpace(A.indptr, A.indices, A.values.detach(), coords, self.coarse_target)
+        self.w = self.weights()
+        self.sw = (self.w.double() * self.G.dinv).to(A.dtype).contiguous()
+        self._fused = self._fused_struct() if A.dtype == torch.float64 else None
         self._setup_key = key
+
+    def _fused_struct(self):
+        """ctypes view of the operator for tm_twolevel_apply (the tensors it
+        points to are kept on self)."""
+        C, G, A = self.coarse, self.G, self.A
+        n = G.n
+        self._sw32 = self.sw.float().contiguous()
+        self._work = torch.empty(2 * n + 4 * C.nc, dtype=torch.float32, device=A.values.device)
+        t = _lib.TwoLevel()
+        t.n, t.nc, t.pad0 = n, C.nc, 0
+        t.agg, t.agg_ptr, t.agg_perm = C.agg32.data_ptr(), C.agg_ptr.data_ptr(), C.agg_order32.data_ptr()
+        t.kc_inv = C.Kc_inv.data_ptr()
+        t.kp_indptr, t.kp_indices, t.kp_values = (C.kp_indptr.data_ptr(), C.kp_indices.data_ptr(),
+                                                  C.kp_values32.data_ptr())
+        t.k_nnz = int(G.values32.shape[0])
+        t.k_indptr, t.k_indices, t.k_values = A.indptr.data_ptr(), A.indices.data_ptr(), G.values32.data_ptr()
+        t.sw, t.work = self._sw32.data_ptr(), self._work.data_ptr()
+        return t
+
+    def weights(self, keep: bool = False):
+        """Smoother weights w (float32 [n]); with keep=True also (y, saved)."""
+        G = self.G
+        if not self.use_network:
+            return torch.ones(G.n, dtype=torch.float32, device=G.aoff.device)
+        x = torch.ones(G.n, dtype=torch.float32, device=G.aoff.device)
+        if keep:
+            y, saved = self.model.forward(G, x, keep=True)
+            return 0.5 + torch.sigmoid(y), (y, saved)
+        return 0.5 + torch.sigmoid(self.model.forward(G, x))
 
     def _K(self, v):
         return spmv_raw(self.A.indptr, self.A.indices, self.A.values, v.to(self.A.dtype).contiguous())
 
-    def smoother(self, r: torch.Tensor) -> torch.Tensor:
-        G = self.G
-        if not self.use_network:
-            return (G.dinv_sqrt.to(r.dtype) ** 2) * r
-        xs = G.dinv_sqrt * r.float()
-        sc = float(torch.linalg.vector_norm(xs)) / math.sqrt(max(1, G.n))
-        if sc == 0.0:
-            return torch.zeros_like(r)
-        y = self.model.forward(G, (xs / sc).contiguous())
-        return (sc * G.dinv_sqrt * y).to(r.dtype)
-
     def __call__(self, r: torch.Tensor) -> torch.Tensor:
-        zc = self.coarse.apply(r)
-        z = zc + self.smoother(r - self._K(zc))
-        return z + self.coarse.apply(r - self._K(z))
+        if self._fused is not None and r.dtype == torch.float64:
+            z = torch.empty_like(r)
+            _lib.call("tm_twolevel_apply", self._fused, r.contiguous().data_ptr(), z.data_ptr(),
+                      _lib.stream_handle(r.device))
+            return z
+        C = self.coarse
+        yc = C.restrict_solve(r)
+        r1 = r - C.kp(yc).to(r.dtype)                 # r - K C r
+        s1 = self.sw * r1                            # S (I - K C) r
+        r2 = self._K(s1)
+        yc2 = C.restrict_solve(r2)
+        return (yc - yc2).to(r.dtype)[C.agg] + s1    # C r + (I - C K) s1
 
-    # -- flexible PCG ------------------------------------------------------------
-    def solve(self, A, b, x, rtol=1e-8, atol=0.0, maxiter=10000, coords=None, check_every: int = 1):
-        """Flexible CG (Polak-Ribiere) with this preconditioner; falls back to
-        Jacobi-PCG if the residual stagnates.  x is updated in place."""
+    def _iterate(self, x, r, p, rz, k: int):
+        """k flexible-PCG iterations; x, r, p and rz (0-dim) are updated in
+        place, so the sequence can be captured once and replayed."""
+        rr, pp, rzz = r, p, rz
+        for _ in range(k):
+            q = self._K(pp)
+            alpha = rzz / torch.dot(pp, q)
+            x.add_(alpha * pp)
+            r_new = rr - alpha * q
+            z_new = self(r_new)
+            beta = torch.clamp(torch.dot(z_new, r_new - rr) / rzz, min=0.0)
+            rzz = torch.dot(r_new, z_new)
+            pp = z_new + beta * pp
+            rr = r_new
+        r.copy_(rr)
+        p.copy_(pp)
+        rz.copy_(rzz)
+
+    def _captured(self, state, k: int):
+        """Capture ``k`` iterations on ``state`` = (x, r, p, rz) as a CUDA graph
+        and return its replay function.  The state tensors are the graph's
+        fixed inputs and outputs: their values change, their storage must not."""
+        x, r, p, rz = state
+        saved = [t.clone() for t in state]
+        side = torch.cuda.Stream(device=x.device)
+        side.wait_stream(torch.cuda.current_stream(x.device))
+        with torch.cuda.stream(side):
+            self._iterate(x, r, p, rz, 1)          # warm-up: library handles, allocator
+        torch.cuda.current_stream(x.device).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._iterate(x, r, p, rz, k)
+        for t, v in zip(state, saved):             # capture records, the warm-up ran: restore
+            t.copy_(v)
+        self._graph = g
+        return g.replay
+
+    def solve(self, A, b, x, rtol=1e-8, atol=0.0, maxiter=10000, coords=None, check_every: int = 8,
+              fallback: bool = True, graph: bool = True):
+        """Flexible CG (Polak-Ribiere beta) with this preconditioner; falls
+        back to Jacobi-PCG if the residual stagnates (``fallback=False``
+        returns after ``maxiter`` iterations instead).  x is updated in place."""
         if coords is None:
             raise ValueError("the learned preconditioner needs dof coordinates (coords=) for its coarse space")
         t0 = time.perf_counter()
         self.setup(A, coords)
         bn = float(torch.linalg.vector_norm(b.double()))
         tol = max(rtol * bn, atol)
-        r = b - self._K(x)
+        xw = x.clone() if graph and x.is_cuda else x
+        r = b - self._K(xw)
         z = self(r)
         p = z.clone()
-        rz = float(torch.dot(r.double(), z.double()))
+        rz = torch.dot(r, z)
         it = 0
         best = float("inf")
         stall = 0
         status = _lib.TM_ERR_MAXITER
+        run = self._captured((xw, r, p, rz), check_every) if xw is not x else None
         while it < maxiter:
-            rn = float(torch.linalg.vector_norm(r.double()))
+            rn = float(torch.linalg.vector_norm(r))
             if rn <= tol:
                 status = _lib.TM_OK
                 break
-            best, stall = (rn, 0) if rn < 0.999 * best else (best, stall + 1)
-            if stall > 50:
-                break
-            q = self._K(p)
-            pq = float(torch.dot(p.double(), q.double()))
-            if not pq > 0:
+            if not math.isfinite(rn):
                 status = _lib.TM_ERR_BREAKDOWN
                 break
-            alpha = rz / pq
-            x += alpha * p
-            r_old = r
-            r = r - alpha * q
-            z_new = self(r)
-            beta = float(torch.dot(z_new.double(), (r - r_old).double())) / rz
-            rz = float(torch.dot(r.double(), z_new.double()))
-            p = z_new + max(beta, 0.0) * p
-            it += 1
+            best, stall = (rn, 0) if rn < 0.999 * best else (best, stall + check_every)
+            if stall > 64:
+                break
+            k = min(check_every, maxiter - it)
+            if run is not None and k == check_every:
+                run()
+            else:
+                self._iterate(xw, r, p, rz, k)
+            it += k
+        if xw is not x:
+            x.copy_(xw)
+        if status == _lib.TM_ERR_MAXITER and float(torch.linalg.vector_norm(r)) <= tol:
+            status = _lib.TM_OK
         true_res = true_relative_residual(A.indptr, A.indices, A.values, b, x, bn)
-        fallback = False
-        if status != _lib.TM_OK or true_res > rtol * 1.0000001:
+        fell_back = False
+        if fallback and (status != _lib.TM_OK or true_res > rtol * 1.0000001):
             fb = pcg_jacobi_raw(A.indptr, A.indices, A.values.contiguous(), b, x, rtol, atol, maxiter)
             it += fb.iterations
-            status, true_res, fallback = fb.status, fb.residual, True
-        return LearnedSolveInfo(status, it, true_res, true_res, 0, "learned", fallback, time.perf_counter() - t0)
+            status, true_res, fell_back = fb.status, fb.residual, True
+        return LearnedSolveInfo(status, it, true_res, true_res, 0, "learned", fell_back, time.perf_counter() - t0)
 
 
 # -- training --------------------------------------------------------------------
-def generate_pairs(systems, checkpoints=(1, 4, 16, 64), rtol=1e-10):
-    """Residual/error pairs of plain Jacobi-PCG iterates.
+def generate_pairs(systems, iterations=(1, 3, 8, 20), rtol=1e-10, coarse_target: int = 512):
+    """Residual/error pairs seen by the preconditioner inside its own solver.
 
-    systems: iterable of (A, b, coords).  For each, the converged solution x*
-    comes from Jacobi-PCG to ``rtol``; then the solver is re-run with an
-    iteration cap k for each checkpoint, giving x_k, e_k = x* - x_k and
-    r_k = b - A x_k."""
-    pairs = []
+    systems: iterable of (A, b, coords).  For each, x* comes from Jacobi-PCG
+    to ``rtol``; then flexible PCG with the two-level method at w = 1 runs and
+    the residual r_k and error e_k = x* - x_k are taken after each count in
+    ``iterations``.  Pairs are grouped per system: (A, coords, [(r, e), ...])."""
+    out = []
     for A, b, coords in systems:
         xs = torch.zeros_like(b)
         pcg_jacobi_raw(A.indptr, A.indices, A.values, b, xs, rtol, 0.0, 100000)
-        for k in checkpoints:
+        base = LearnedPreconditioner(None, device=b.device, coarse_target=coarse_target, use_network=False)
+        pr = []
+        for k in iterations:
             xk = torch.zeros_like(b)
-            pcg_jacobi_raw(A.indptr, A.indices, A.values, b, xk, 1e-30, 0.0, k, max_restarts=0)
-            e = (xs - xk).float()
-            r = (b - spmv_raw(A.indptr, A.indices, A.values, xk)).float()
-            pairs.append((A, coords, r, e))
-    return pairs
+            base.solve(A, b, xk, rtol=1e-30, maxiter=k, coords=coords, check_every=k, fallback=False, graph=False)
+            r = b - spmv_raw(A.indptr, A.indices, A.values, xk)
+            pr.append((r.float(), (xs - xk).float()))
+        out.append((A, coords, pr))
+    return out
 
 
 class Adam:
@@ -335,41 +451,47 @@ class Adam:
             self.p[k] -= self.lr * mh / (vh.sqrt() + self.eps)
 
 
-def train(precond: LearnedPreconditioner, pairs, epochs: int = 2, lr: float = 2e-3, log=None) -> List[float]:
-    """Minimise E ||z(r) - e||_K^2 / ||e||_K^2 over the pairs, where z is the
-    two-level preconditioner's output and only the network is trained."""
+def train(precond: LearnedPreconditioner, systems, epochs: int = 2, lr: float = 2e-3, log=None) -> List[float]:
+    """Minimise the mean over pairs of ||z(r) - e||_K^2 / ||e||_K^2, z the
+    preconditioner's output, over the network that sets the smoother weights.
+
+    With s = S r1, r1 = (I - K C) r and z = C r + (I - C K) s, the gradient
+    of the loss L with respect to s is g_s = (I - K C) g_z (C, K symmetric),
+    g_z = 2 K (z - e) / ||e||_K^2, so dL/dw_i = g_s,i (D^-1 r1)_i and
+    dL/dy_i = dL/dw_i * (w_i - 1/2) (3/2 - w_i).  Per system the network runs
+    forward once and backward once on the summed gradient."""
     model = precond.model
+    precond.use_network = True
     opt = Adam(model.params, lr=lr)
     losses = []
     for ep in range(epochs):
-        for (A, coords, r, e) in pairs:
+        for (A, coords, pr) in systems:
+            precond._setup_key = None
             precond.setup(A, coords)
-            G = precond.G
-            A32 = G.values32
-            K = lambda v: spmv_raw(A.indptr, A.indices, A32, v.contiguous())  # noqa: E731
-            zc = precond.coarse.apply(r)
-            r1 = r - K(zc)
-            xs = G.dinv_sqrt * r1
-            sc = float(torch.linalg.vector_norm(xs)) / math.sqrt(G.n)
-            if sc == 0.0:
-                continue
-            y, saved = model.forward(G, (xs / sc).contiguous(), keep=True)
-            zs = sc * G.dinv_sqrt * y
-            z1 = zc + zs
-            z = z1 + precond.coarse.apply(r - K(z1))
-            err = z - e
-            Ke = K(e)
-            enorm = float(torch.dot(e, Ke))
-            Kerr = K(err)
-            loss = float(torch.dot(err, Kerr)) / enorm
-            losses.append(loss)
-            # d loss / d z = 2 K err / enorm ; z = z1 + C (r - K z1) => dz1 = (I - K C) dz (C, K symmetric)
-            gz = 2.0 * Kerr / enorm
-            gz1 = gz - K(precond.coarse.apply(gz))
-            gy = sc * G.dinv_sqrt * gz1
+            G, C = precond.G, precond.coarse
+            w, (y, saved) = precond.weights(keep=True)
+            dinv = G.dinv.float()
+            K = lambda v: spmv_raw(A.indptr, A.indices, A.values, v.double().contiguous()).float()  # noqa: E731
+            gy = torch.zeros_like(y)
+            for r, e in pr:
+                yc = C.restrict_solve(r)
+                r1 = r - C.kp(yc).float()
+                u = dinv * r1                         # D^-1 r1
+                s = w * u
+                z = yc.float()[C.agg] + s - C.apply(K(s)).float()
+                err = z - e
+                Kerr = K(err)
+                enorm = float(torch.dot(e, K(e)))
+                if not enorm > 0:
+                    continue
+                losses.append(float(torch.dot(err, Kerr)) / enorm)
+                gz = 2.0 * Kerr / enorm
+                gs = gz - K(C.apply(gz).float())
+                gy += gs * u * (w - 0.5) * (1.5 - w) / len(pr)
             grads = model.backward(G, saved, gy)
             opt.step(grads)
             model.invalidate()
         if log is not None:
-            log(ep, sum(losses[-len(pairs):]) / max(1, len(pairs)))
+            n_pairs = sum(len(pr) for _, _, pr in systems)
+            log(ep, sum(losses[-n_pairs:]) / max(1, n_pairs))
     return losses

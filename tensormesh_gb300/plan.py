@@ -134,6 +134,30 @@ def rcb_partition(coords: torch.Tensor, n_levels: int = None, n_parts: int = Non
     return part
 
 
+def morton_parts(coords: torch.Tensor, target: int) -> torch.Tensor:
+    """Spatially compact parts of ``target`` points: points sorted along a
+    Z-order (Morton) curve of their coordinates quantised to 2^21 cells per
+    axis over the bounding box, cut into consecutive runs.  One sort instead
+    of one per bisection level; part ids follow the curve."""
+    N, D = coords.shape
+    dev = coords.device
+    if N == 0:
+        return torch.zeros(0, dtype=torch.int64, device=dev)
+    c = coords.to(torch.float64)
+    lo, hi = c.min(0).values, c.max(0).values
+    bits = 63 // D
+    q = ((c - lo) / torch.clamp(hi - lo, min=1e-300) * ((1 << bits) - 1)).round().long()
+    key = torch.zeros(N, dtype=torch.int64, device=dev)
+    for b in range(bits):
+        for d in range(D):
+            key |= ((q[:, d] >> b) & 1) << (b * D + d)
+    order = torch.argsort(key, stable=True)
+    n_parts = max(1, (N + target - 1) // target)
+    part = torch.empty(N, dtype=torch.int64, device=dev)
+    part[order] = torch.arange(N, device=dev) * n_parts // N
+    return part
+
+
 def rcb_partition_grouped(coords: torch.Tensor, groups: torch.Tensor, weight: torch.Tensor,
                           budget: float, max_rows: int):
     """RCB inside fixed groups (e.g. the instances of a batch): segments start

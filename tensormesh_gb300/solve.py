@@ -42,7 +42,8 @@ def spmv_raw(indptr, indices, values, x, out=None):
     n = indptr.shape[0] - 1
     if out is None:
         out = torch.empty(n, dtype=values.dtype, device=values.device)
-    _lib.call("tm_spmv_csr", _dt(values), n, indptr.data_ptr(), indices.data_ptr(), values.data_ptr(),
+    _lib.call("tm_spmv_csr", _dt(values), n, int(values.shape[0]), indptr.data_ptr(), indices.data_ptr(),
+              values.data_ptr(),
               x.data_ptr(), out.data_ptr(), _lib.stream_handle(values.device))
     return out
 

@@ -6,9 +6,11 @@ Each training system is a 3D P1 Poisson problem on an n^3 Kuhn cube, with
 log kappa piecewise constant on 8^3 blocks, each block N(0, 2^2), zero
 Dirichlet on all faces and f = 1: the generator of the 128^3 benchmark
 configuration at a smaller size, with fresh seeds.  Residual/error pairs come
-from the plain Jacobi-PCG iterates of each system (``learned.generate_pairs``),
-and the network is trained with the project's own forward/backward kernels
-(``learned.train``).  The weights are written as an .npz of float32 arrays.
+from the preconditioner's own flexible-PCG iterates (two-level method with
+unit smoother weights) on each system (``learned.generate_pairs``), and the
+network that sets the smoother weights is trained with the project's own
+forward/backward kernels (``learned.train``).  The weights are written as an
+.npz of float32 arrays.
 """
 from __future__ import annotations
 
@@ -78,25 +80,28 @@ def main():
     ap.add_argument("--epochs", type=int, default=2)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--coarse", type=int, default=512, help="dofs per coarse aggregate")
-    ap.add_argument("--checkpoints", default="2,8,32")
+    ap.add_argument("--iterations", default="1,3,8,20", help="flexible-PCG iteration counts of the pairs")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", required=True)
     args = ap.parse_args()
     torch.cuda.set_device(0)
     fam = PoissonFamily(args.n)
     t0 = time.perf_counter()
-    cps = tuple(int(c) for c in args.checkpoints.split(","))
-    pairs = []
+    its = tuple(int(c) for c in args.iterations.split(","))
+    systems = []
     for s in range(args.systems):
-        pairs += generate_pairs([fam.system(10_000 + s)], checkpoints=cps)
+        systems += generate_pairs([fam.system(10_000 + s)], iterations=its, coarse_target=args.coarse)
     t_data = time.perf_counter() - t0
-    pre = LearnedPreconditioner(MPNN("cuda", seed=args.seed), coarse_target=args.coarse)
+    model = MPNN("cuda", seed=args.seed)
+    model.params["wr"].zero_()          # start from w = 1 (the method without the network)
+    pre = LearnedPreconditioner(model, coarse_target=args.coarse)
     log = []
-    losses = train(pre, pairs, epochs=args.epochs, lr=args.lr,
+    losses = train(pre, systems, epochs=args.epochs, lr=args.lr,
                    log=lambda ep, l: log.append((ep, l)) or print(f"epoch {ep}: mean loss {l:.4f}", flush=True))
     t_train = time.perf_counter() - t0 - t_data
+    n_pairs = sum(len(pr) for _, _, pr in systems)
     meta = dict(systems=args.systems, n=args.n, epochs=args.epochs, lr=args.lr, coarse=args.coarse,
-                checkpoints=list(cps), pairs=len(pairs), data_seconds=t_data, train_seconds=t_train,
+                iterations=list(its), pairs=n_pairs, data_seconds=t_data, train_seconds=t_train,
                 first_epoch_loss=log[0][1] if log else None, last_epoch_loss=log[-1][1] if log else None)
     save_weights(pre.model, args.out, meta)
     print(json.dumps(meta))
