@@ -18,10 +18,11 @@ w = 1/2 + sigmoid(y):
     z = C r + (I - C K) S (I - K C) r.
 The network runs once per matrix, at set-up; an iteration costs two SpMVs
 (K and the thin K P), two coarse solves and vector updates, all on the device
-without host synchronisation.  Training minimises the energy norm
-||z(r_k) - e_k||_K^2 / ||e_k||_K^2 over residual/error pairs taken from the
-preconditioner's own flexible-PCG iterates on generated systems, with the
-hand-written forward and backward kernels and Adam.  The true FP64 residual
+without host synchronisation.  Training minimises a proxy of the condition
+number of the preconditioned operator (Rayleigh quotients of errors taken
+from the preconditioner's own flexible-PCG iterates against those of random
+errors, see ``train``) on generated systems, with the hand-written forward
+and backward kernels and Adam.  The true FP64 residual
 ||b - K x|| / ||b|| decides convergence, and a stagnating solve falls back to
 Jacobi-PCG.
 """
@@ -451,18 +452,29 @@ class Adam:
             self.p[k] -= self.lr * mh / (vh.sqrt() + self.eps)
 
 
-def train(precond: LearnedPreconditioner, systems, epochs: int = 2, lr: float = 2e-3, log=None) -> List[float]:
-    """Minimise the mean over pairs of ||z(r) - e||_K^2 / ||e||_K^2, z the
-    preconditioner's output, over the network that sets the smoother weights.
+def train(precond: LearnedPreconditioner, systems, epochs: int = 2, lr: float = 2e-3, log=None,
+          n_random: int = 4, seed: int = 0) -> List[float]:
+    """Fit the network that sets the smoother weights by a condition-number
+    proxy of the preconditioned operator M K.
 
-    With s = S r1, r1 = (I - K C) r and z = C r + (I - C K) s, the gradient
-    of the loss L with respect to s is g_s = (I - K C) g_z (C, K symmetric),
-    g_z = 2 K (z - e) / ||e||_K^2, so dL/dw_i = g_s,i (D^-1 r1)_i and
-    dL/dy_i = dL/dw_i * (w_i - 1/2) (3/2 - w_i).  Per system the network runs
+    For an error e with residual r = K e, rho(e) = r^T M r / e^T K e lies in
+    [lambda_min, lambda_max] of M K.  The errors of the solver's own iterates
+    sit near lambda_min and random errors spread over the spectrum, so the
+    loss per system is mean(-log rho) over the iterate pairs plus
+    mean(log rho) over ``n_random`` Gaussian errors: a proxy for
+    log(lambda_max / lambda_min), the quantity PCG's iteration count follows.
+    (A common scale of the weights does not change it: the coarse part of M K
+    is the identity on its own K-orthogonal subspace.)
+
+    With s = S r1, r1 = (I - K C) r, z = M r = C r + (I - C K) s and
+    d log(r^T z) / dz = r / r^T z, the gradient with respect to s is
+    (I - K C) r / r^T z, so dL/dw_i = g_s,i (D^-1 r1)_i and
+    dL/dy_i = dL/dw_i (w_i - 1/2) (3/2 - w_i).  Per system the network runs
     forward once and backward once on the summed gradient."""
     model = precond.model
     precond.use_network = True
     opt = Adam(model.params, lr=lr)
+    gen = torch.Generator(device="cpu").manual_seed(seed)
     losses = []
     for ep in range(epochs):
         for (A, coords, pr) in systems:
@@ -473,25 +485,26 @@ def train(precond: LearnedPreconditioner, systems, epochs: int = 2, lr: float = 
             dinv = G.dinv.float()
             K = lambda v: spmv_raw(A.indptr, A.indices, A.values, v.double().contiguous()).float()  # noqa: E731
             gy = torch.zeros_like(y)
-            for r, e in pr:
+            rand = [torch.randn(G.n, generator=gen).to(y.device) for _ in range(n_random)]
+            terms = [(r, e, -1.0 / len(pr)) for r, e in pr] + [(K(e), e, 1.0 / n_random) for e in rand]
+            total = 0.0
+            for r, e, sgn in terms:
                 yc = C.restrict_solve(r)
                 r1 = r - C.kp(yc).float()
                 u = dinv * r1                         # D^-1 r1
                 s = w * u
                 z = yc.float()[C.agg] + s - C.apply(K(s)).float()
-                err = z - e
-                Kerr = K(err)
-                enorm = float(torch.dot(e, K(e)))
-                if not enorm > 0:
+                rz = float(torch.dot(r, z))
+                eke = float(torch.dot(e, K(e)))
+                if not (rz > 0 and eke > 0):
                     continue
-                losses.append(float(torch.dot(err, Kerr)) / enorm)
-                gz = 2.0 * Kerr / enorm
-                gs = gz - K(C.apply(gz).float())
-                gy += gs * u * (w - 0.5) * (1.5 - w) / len(pr)
+                total += sgn * math.log(rz / eke)
+                gs = (r - K(C.apply(r).float())) * (sgn / rz)
+                gy += gs * u * (w - 0.5) * (1.5 - w)
+            losses.append(total)
             grads = model.backward(G, saved, gy)
             opt.step(grads)
             model.invalidate()
         if log is not None:
-            n_pairs = sum(len(pr) for _, _, pr in systems)
-            log(ep, sum(losses[-n_pairs:]) / max(1, n_pairs))
+            log(ep, sum(losses[-len(systems):]) / max(1, len(systems)))
     return losses

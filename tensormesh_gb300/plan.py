@@ -135,10 +135,12 @@ def rcb_partition(coords: torch.Tensor, n_levels: int = None, n_parts: int = Non
 
 
 def morton_parts(coords: torch.Tensor, target: int) -> torch.Tensor:
-    """Spatially compact parts of ``target`` points: points sorted along a
-    Z-order (Morton) curve of their coordinates quantised to 2^21 cells per
-    axis over the bounding box, cut into consecutive runs.  One sort instead
-    of one per bisection level; part ids follow the curve."""
+    """Spatially compact parts of about ``target`` points: the cells of an
+    octree (quadtree in 2D) over the bounding box, refined where a cell holds
+    more than 2 * target points.  Points are sorted once along the Z-order
+    (Morton) curve of their coordinates quantised to 2^(63 // D) steps per
+    axis; every cell is then a run of that order, identified by a key prefix.
+    Part ids follow the curve."""
     N, D = coords.shape
     dev = coords.device
     if N == 0:
@@ -152,9 +154,21 @@ def morton_parts(coords: torch.Tensor, target: int) -> torch.Tensor:
         for d in range(D):
             key |= ((q[:, d] >> b) & 1) << (b * D + d)
     order = torch.argsort(key, stable=True)
-    n_parts = max(1, (N + target - 1) // target)
+    k = key[order]
+    level0 = max(0, min(bits, int(math.floor(math.log(max(1.0, N / target)) / math.log(2 ** D)))))
+    level = torch.full((N,), level0, dtype=torch.int64, device=dev)
+    for _ in range(bits + 1):
+        prefix = k >> (D * (bits - level))
+        new = torch.ones(N, dtype=torch.bool, device=dev)
+        new[1:] = (prefix[1:] != prefix[:-1]) | (level[1:] != level[:-1])
+        seg = torch.cumsum(new.long(), 0) - 1
+        counts = torch.bincount(seg)
+        over = (counts[seg] > 2 * target) & (level < bits)
+        if not bool(over.any()):
+            break
+        level = level + over.long()
     part = torch.empty(N, dtype=torch.int64, device=dev)
-    part[order] = torch.arange(N, device=dev) * n_parts // N
+    part[order] = seg
     return part
 
 

@@ -1,6 +1,6 @@
 """Train the learned preconditioner's message-passing network on the GPU.
 
-    python -m tensormesh_gb300.train_learned --systems 2000 --n 32 --out weights.npz
+    python -m tensormesh_gb300.train_learned --systems 500 --epochs 4 --lr 5e-4 --n 32 --out weights.npz
 
 Each training system is a 3D P1 Poisson problem on an n^3 Kuhn cube, with
 log kappa piecewise constant on 8^3 blocks, each block N(0, 2^2), zero
@@ -9,8 +9,11 @@ configuration at a smaller size, with fresh seeds.  Residual/error pairs come
 from the preconditioner's own flexible-PCG iterates (two-level method with
 unit smoother weights) on each system (``learned.generate_pairs``), and the
 network that sets the smoother weights is trained with the project's own
-forward/backward kernels (``learned.train``).  The weights are written as an
-.npz of float32 arrays.
+forward/backward kernels (``learned.train``).  After every epoch the network
+is scored by the mean flexible-PCG iteration count on held-out systems of the
+same generator; the best checkpoint is kept, the untrained network (weights
+w = 1, the method without learning) being checkpoint 0.  The weights are
+written as an .npz of float32 arrays, the selection record in its metadata.
 """
 from __future__ import annotations
 
@@ -82,6 +85,7 @@ def main():
     ap.add_argument("--coarse", type=int, default=512, help="dofs per coarse aggregate")
     ap.add_argument("--iterations", default="1,3,8,20", help="flexible-PCG iteration counts of the pairs")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--val", type=int, default=4, help="held-out systems for checkpoint selection")
     ap.add_argument("--out", required=True)
     args = ap.parse_args()
     torch.cuda.set_device(0)
@@ -95,14 +99,37 @@ def main():
     model = MPNN("cuda", seed=args.seed)
     model.params["wr"].zero_()          # start from w = 1 (the method without the network)
     pre = LearnedPreconditioner(model, coarse_target=args.coarse)
+    val = [fam.system(90_000 + s) for s in range(args.val)]
+
+    def val_iterations() -> float:
+        its = []
+        for A, b, coords in val:
+            p = LearnedPreconditioner(model, coarse_target=args.coarse)
+            its.append(p.solve(A, b, torch.zeros_like(b), rtol=1e-8, coords=coords, check_every=1).iterations)
+        return float(np.mean(its))
+
+    # checkpoint selection on the solver's own metric: flexible-PCG iterations
+    # on held-out systems; the initial network (w = 1) is checkpoint 0
+    history = [(0, val_iterations(), None)]
+    best = (history[0][1], {k: v.clone() for k, v in model.params.items()})
     log = []
-    losses = train(pre, systems, epochs=args.epochs, lr=args.lr,
-                   log=lambda ep, l: log.append((ep, l)) or print(f"epoch {ep}: mean loss {l:.4f}", flush=True))
+    for ep in range(args.epochs):
+        train(pre, systems, epochs=1, lr=args.lr, seed=args.seed + ep,
+              log=lambda _, l: log.append((ep, l)) or print(f"epoch {ep}: mean loss {l:.4f}", flush=True))
+        v = val_iterations()
+        history.append((ep + 1, v, log[-1][1] if log else None))
+        print(f"epoch {ep}: validation iterations {v:.1f}", flush=True)
+        if v < best[0]:
+            best = (v, {k: t.clone() for k, t in model.params.items()})
+    for k, t in best[1].items():
+        model.params[k].copy_(t)
+    model.invalidate()
     t_train = time.perf_counter() - t0 - t_data
     n_pairs = sum(len(pr) for _, _, pr in systems)
     meta = dict(systems=args.systems, n=args.n, epochs=args.epochs, lr=args.lr, coarse=args.coarse,
                 iterations=list(its), pairs=n_pairs, data_seconds=t_data, train_seconds=t_train,
-                first_epoch_loss=log[0][1] if log else None, last_epoch_loss=log[-1][1] if log else None)
+                validation=[dict(checkpoint=c, mean_iterations=v, train_loss=l) for c, v, l in history],
+                selected_validation_iterations=best[0])
     save_weights(pre.model, args.out, meta)
     print(json.dumps(meta))
 

@@ -118,10 +118,9 @@ def test_training_and_two_level_solve_against_jacobi_pcg():
     model.params["wr"].zero_()
     pre = LearnedPreconditioner(model, coarse_target=64)
     losses = train(pre, systems, epochs=3, lr=3e-3)
-    n_pairs = sum(len(pr) for _, _, pr in systems)
-    assert len(losses) == 3 * n_pairs and all(math.isfinite(v) for v in losses)
-    # one untrained pass of the loss is the method without the network (w = 1)
-    assert all(0.0 < v < 1.5 for v in losses[:n_pairs])
+    assert len(losses) == 3 * len(systems) and all(math.isfinite(v) for v in losses)
+    # the proxy is log(lambda_max / lambda_min) up to the sampling: positive
+    assert all(v > 0.0 for v in losses)
     K, f, coords = poisson_system(16, 99)
     K.solve(f, rtol=1e-8)
     jac_its = K.last_solve_info.iterations
