@@ -55,17 +55,22 @@ def algorithmic_bytes(E, B, D, N, nnz, itemsize=8):
     return 4 * B * E + itemsize * D * N + itemsize * E + itemsize * nnz
 
 
-def read_profile_traffic():
+def read_profile_value(prefix: str):
+    """A number from the committed ncu summary of the headline kernel."""
     path = os.path.join(ROOT, "profiles", "assemble_p1tet_fp64_128cube.txt")
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith("dram_bytes_per_launch_full_size:"):
+        if line.startswith(prefix):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def read_profile_traffic():
+    return read_profile_value("dram_bytes_per_launch_full_size:")
 
 
 class ClockSampler:
@@ -216,10 +221,12 @@ def run_ours(args):
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record(stream)
+    torch.cuda.nvtx.range_push("bench_timed")   # lets a profiler select exactly the timed launches
     for i in range(args.steps):
         ev[i][0].record(stream)
         step()
         ev[i][1].record(stream)
+    torch.cuda.nvtx.range_pop()
     t1.record(stream)
     torch.cuda.synchronize()
     if world > 1:
@@ -317,25 +324,35 @@ def run_ours(args):
                    "setup_seconds": setup_b, "gpu_launches_per_step": 1}
         del bp, meshes
 
-    # ---- end to end through the public API with host buffers
+    # ---- end to end through the public API with host buffers: every step
+    #      copies its inputs from pinned host memory, assembles, and reads the
+    #      CSR values back; consecutive steps alternate between two streams so
+    #      one step's copies overlap the neighbouring steps' work
     pts_h = mesh.points.cpu().pin_memory()
     kap_h = kappa_h.pin_memory()
-    out_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+    outs_h = [torch.empty(nnz, dtype=torch.float64).pin_memory() for _ in streams]
 
-    def e2e_step():
-        p = pts_h.to(dev, non_blocking=True)
-        k = kap_h.to(dev, non_blocking=True)
-        v = asm(p, element_data={"kappa": k}).values
-        out_h.copy_(v, non_blocking=True)
+    def e2e_step(i):
+        st = streams[i % 2]
+        with torch.cuda.stream(st):
+            p = pts_h.to(dev, non_blocking=True)
+            k = kap_h.to(dev, non_blocking=True)
+            v = asm(p, element_data={"kappa": k}).values
+            outs_h[i % 2].copy_(v, non_blocking=True)
 
-    for _ in range(2):
-        e2e_step()
+    for i in range(2):
+        e2e_step(i)
     torch.cuda.synchronize()
     s0 = torch.cuda.Event(enable_timing=True)
     s1 = torch.cuda.Event(enable_timing=True)
     s0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
+    for st in streams:
+        st.wait_stream(stream)
+    for i in range(args.steps):
+        e2e_step(i)
+    for st in streams:
+        stream.wait_stream(st)
     s1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = s0.elapsed_time(s1) / args.steps
@@ -429,9 +446,12 @@ def run_ours(args):
                        "setup_seconds": round(setup_s, 3)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
-                         "algorithmic_bytes_per_launch": alg, "kernel_ms": kernel_ms},
+                         "algorithmic_bytes_per_launch": alg, "kernel_ms": kernel_ms,
+                         "ncu_issue_active_pct": read_profile_value("smsp__issue_active.avg.pct_of_peak_sustained_active:"),
+                         "limiter": "instruction issue (double-float arithmetic on the FP32 pipe), not HBM"},
             "e2e": {"value": world * E / (e2e_ms * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                    "pipelining": "consecutive steps on two alternating streams"},
             "cpu_baseline": cpu,
             "fp32_variant": fp32,
             "elasticity_c2": elast,
