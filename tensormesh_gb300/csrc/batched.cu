@@ -51,7 +51,9 @@ struct BatchArgs {
 };
 
 constexpr int kBatchThreads = 512;
-constexpr int kRowIlp = 8;  // CSR entries fetched together per row (P1 triangles: 7 per interior row)
+constexpr int kRowIlp = 4;  // CSR entries fetched together per row and round
+constexpr int kRows = 2;    // rows a thread advances together in the SpMV
+constexpr int kVec = 4;     // rows a thread advances together in the vector update
 
 __device__ __forceinline__ double cta_sum(double v, double* red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -98,7 +100,7 @@ __device__ __forceinline__ double cluster_combine(cg::cluster_group& cl, double*
 }
 
 template <int EL>
-__global__ void __launch_bounds__(kBatchThreads) batched_assemble_pcg_kernel(BatchArgs A) {
+__global__ void __launch_bounds__(kBatchThreads, 2) batched_assemble_pcg_kernel(BatchArgs A) {
   cg::cluster_group cl = cg::this_cluster();
   const unsigned rank = cl.block_rank();
   const unsigned C = cl.num_blocks();
@@ -180,29 +182,53 @@ __global__ void __launch_bounds__(kBatchThreads) batched_assemble_pcg_kernel(Bat
       }
       if (it == A.maxiter) break;
       double pq_l = 0;
-      // one thread per row; each row's entries are fetched kRowIlp at a time
-      // (all loads of a chunk issued before the first use), so a warp keeps
-      // 32 x kRowIlp independent gathers in flight instead of one chain
-      for (int64_t row = r0 + threadIdx.x; row < r1; row += kBatchThreads) {
-        const int64_t k0 = A.indptr[row], k1 = A.indptr[row + 1];
-        float s = 0.f;
-        for (int64_t kb = k0; kb < k1; kb += kRowIlp) {
-          int c[kRowIlp];
-          float v[kRowIlp];
+      // one thread per row, kRows rows at a time (rows row, row + T, ...), each
+      // row's entries fetched kRowIlp at a time with every load of the round
+      // issued before the first use: a warp keeps 32 x kRows x kRowIlp
+      // independent gathers in flight instead of one dependent chain per row
+      for (int64_t base = r0 + threadIdx.x; base < r1; base += kRows * kBatchThreads) {
+        int64_t k0[kRows], k1[kRows];
+        float s[kRows];
 #pragma unroll
-          for (int j = 0; j < kRowIlp; ++j) {
-            const bool ok = kb + j < k1;
-            c[j] = ok ? A.indices[kb + j] : (int)row;
-            v[j] = ok ? val[kb + j] : 0.f;
-          }
-#pragma unroll
-          for (int j = 0; j < kRowIlp; ++j) s += v[j] * (A.z[c[j]] + beta * pold[c[j]]);
+        for (int u = 0; u < kRows; ++u) {
+          const int64_t row = base + (int64_t)u * kBatchThreads;
+          const bool ok = row < r1;
+          k0[u] = ok ? A.indptr[row] : 0;
+          k1[u] = ok ? A.indptr[row + 1] : 0;
+          s[u] = 0.f;
         }
-        const bool fixed = A.dirichlet[row] != 0;
-        const float pv = A.z[row] + beta * pold[row];
-        const float qv = fixed ? 0.f : s;
-        A.q[row] = qv;
-        pq_l += (double)pv * qv;
+        for (int64_t j0 = 0;; j0 += kRowIlp) {
+          bool more = false;
+#pragma unroll
+          for (int u = 0; u < kRows; ++u) more |= k0[u] + j0 < k1[u];
+          if (!more) break;
+          int c[kRows][kRowIlp];
+          float v[kRows][kRowIlp];
+#pragma unroll
+          for (int u = 0; u < kRows; ++u)
+#pragma unroll
+            for (int j = 0; j < kRowIlp; ++j) {
+              const int64_t kk = k0[u] + j0 + j;
+              const bool ok = kk < k1[u];
+              c[u][j] = ok ? A.indices[kk] : (int)r0;
+              v[u][j] = ok ? val[kk] : 0.f;
+            }
+#pragma unroll
+          for (int u = 0; u < kRows; ++u)
+#pragma unroll
+            for (int j = 0; j < kRowIlp; ++j) s[u] += v[u][j] * (A.z[c[u][j]] + beta * pold[c[u][j]]);
+        }
+#pragma unroll
+        for (int u = 0; u < kRows; ++u) {
+          const int64_t row = base + (int64_t)u * kBatchThreads;
+          if (row < r1) {
+            const bool fixed = A.dirichlet[row] != 0;
+            const float pv = A.z[row] + beta * pold[row];
+            const float qv = fixed ? 0.f : s[u];
+            A.q[row] = qv;
+            pq_l += (double)pv * qv;
+          }
+        }
       }
       t0 = cta_sum(pq_l, red);
       if (threadIdx.x == 0) part[par][0] = t0;
@@ -215,16 +241,37 @@ __global__ void __launch_bounds__(kBatchThreads) batched_assemble_pcg_kernel(Bat
       }
       const float alpha = (float)(rz / pq);
       double rz_n = 0, rr_n = 0;
-      for (int64_t row = r0 + threadIdx.x; row < r1; row += kBatchThreads) {
-        const float pv = A.z[row] + beta * pold[row];
-        pnew[row] = pv;
-        A.x[row] += alpha * pv;
-        const float rv = A.r[row] - alpha * A.q[row];
-        A.r[row] = rv;
-        const float zv = A.dinv[row] * rv;
-        A.z[row] = zv;
-        rz_n += (double)rv * zv;
-        rr_n += (double)rv * rv;
+      // kVec rows per round, every load of the round before any store (the
+      // vectors are distinct arrays, but the compiler cannot know that and
+      // would otherwise serialise the rows behind one another's stores)
+      for (int64_t base = r0 + threadIdx.x; base < r1; base += kVec * kBatchThreads) {
+        float zz[kVec], po[kVec], xx[kVec], rr[kVec], qq[kVec], di[kVec];
+#pragma unroll
+        for (int u = 0; u < kVec; ++u) {
+          const int64_t row = base + (int64_t)u * kBatchThreads;
+          const bool ok = row < r1;
+          zz[u] = ok ? A.z[row] : 0.f;
+          po[u] = ok ? pold[row] : 0.f;
+          xx[u] = ok ? A.x[row] : 0.f;
+          rr[u] = ok ? A.r[row] : 0.f;
+          qq[u] = ok ? A.q[row] : 0.f;
+          di[u] = ok ? A.dinv[row] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kVec; ++u) {
+          const int64_t row = base + (int64_t)u * kBatchThreads;
+          if (row < r1) {
+            const float pv = zz[u] + beta * po[u];
+            const float rv = rr[u] - alpha * qq[u];
+            const float zv = di[u] * rv;
+            pnew[row] = pv;
+            A.x[row] = xx[u] + alpha * pv;
+            A.r[row] = rv;
+            A.z[row] = zv;
+            rz_n += (double)rv * zv;
+            rr_n += (double)rv * rv;
+          }
+        }
       }
       cta_sum2(rz_n, rr_n, red2);
       if (threadIdx.x == 0) {
