@@ -272,6 +272,7 @@ def run_ours(args):
 
     # ---- C2: 64^3 P1-tet linear elasticity, per-element E, FP64 (secondary)
     elast = None
+    hyper = None
     if not args.no_extra:
         m2 = tg.Mesh.gen_unit_cube(64, device=dev)
         rng = np.random.default_rng(SEED + 2)
@@ -289,7 +290,20 @@ def run_ours(args):
         elast = {"workload": "64^3 Kuhn cube P1-tet elasticity, per-element E = exp(0.5 g), nu = 0.3, FP64",
                  "elements_per_s": t2.n_elements / (ms2 * 1e-3), "kernel_ms": ms2, "algorithmic_bytes": alg2,
                  "achieved_gbs": alg2 / (ms2 * 1e-3) / 1e9}
-        del easm, m2
+        # Neo-Hookean energy + its displacement gradient (ElementAssembler.energy
+        # and backward) on the same mesh
+        nh = tg.NeoHookeanModel.from_mesh(m2, quadrature_order=1, E=1.0, nu=0.3)
+        g_u = torch.from_numpy(np.random.default_rng(SEED + 5).normal(size=tuple(m2.points.shape)))
+        u_nh = (g_u * (0.1 / 64)).to(dev).requires_grad_(True)
+
+        def nh_step():
+            u_nh.grad = None
+            nh.energy(u_nh).backward()
+        ms_nh = time_calls(nh_step)
+        hyper = {"workload": "64^3 Kuhn cube, Neo-Hookean energy and its displacement gradient, FP64, "
+                             "u ~ N(0, (0.1 h)^2) per node",
+                 "elements_per_s": t2.n_elements / (ms_nh * 1e-3), "ms_per_energy_and_gradient": ms_nh}
+        del easm, m2, nh
 
     # ---- C3: 256 uneven 2D Poisson meshes, assembled + Jacobi-PCG in one
     #      persistent, graph-captured launch (FP32), autotuned launch shape
@@ -455,6 +469,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "fp32_variant": fp32,
             "elasticity_c2": elast,
+            "neo_hookean_energy": hyper,
             "batched_c3": batched,
             "gpu_launches": args.steps,
             "clocks": clk,

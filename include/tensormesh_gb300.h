@@ -259,6 +259,19 @@ typedef struct tm_twolevel {
 
 int tm_twolevel_apply(const tm_twolevel* t, const double* r, double* z, void* stream);
 
+/*
+ * Neo-Hookean energy per element and its displacement gradient per (element,
+ * local node) (replaces NeoHookeanModel.energy, assemble/builtin.py:220-334,
+ * the quadrature loop of ElementAssembler.energy, element_assembler.py:
+ * 468-680, and the autograd of both).  tables: the flat [w(Q), N(Q*B),
+ * dN(Q*B*D)] float64 table; points and u are [N][D] in dtype; energy_el
+ * [n_elements] float64; grad_el [n_elements][B][D] in dtype, or NULL for the
+ * energy alone.  mu, lam: Lame constants.  FP64 arithmetic in the kernel.
+ */
+int tm_neohookean(int32_t element, int32_t dtype, int32_t n_quad, const double* tables, const void* points,
+                  const int32_t* elements, int64_t n_elements, const void* u, double mu, double lam,
+                  double* energy_el, void* grad_el, void* stream);
+
 /* y = A x for CSR A (replaces SparseMatrix @ / spmv, sparse/mm/__init__.py:
  * 22-72).  dtype applies to values, x and y; nnz = indptr[n_rows] (it sets
  * the lanes per row; the row extents come from indptr). */

@@ -458,3 +458,38 @@ def compliance_gradients_kappa(points, elements, element_type, quadrature_order,
     ue = u[elements]
     lam = u  # symmetric K and J = b^T u  =>  adjoint = u
     return -np.einsum("ei,eij,ej->e", lam[elements], K0, ue)
+
+
+def neo_hookean(points, elements, element_type, quadrature_order, u, E=1.0, nu=0.3):
+    """Neo-Hookean energy and its gradient with respect to the nodal
+    displacement u [N, D] (assemble/builtin.py:220-334, NeoHookeanModel;
+    ElementAssembler.energy, element_assembler.py:468-680).
+
+    psi(F) = mu/2 (tr F^T F - d) - mu ln J + lam/2 (ln J)^2 with F = I + grad u,
+    grad u[i][j] = sum_b u_b[i] dN_b/dx_j ("eb...,eqbd->eq...d"), J = det F,
+    mu = E / (2 (1 + nu)), lam = E nu / ((1 + nu)(1 - 2 nu)) (Python floats);
+    energy = sum over elements and quadrature points of psi * w |det J_x|.
+    The gradient is the first Piola-Kirchhoff stress P = mu F + (lam ln J - mu)
+    F^-T contracted with the shape gradients: dE/du_b[i] = sum_q JxW P[i][d]
+    dN_b/dx_d, scattered to the nodes (what autograd of the energy returns).
+    """
+    w, xi = quadrature(element_type, quadrature_order)
+    _, dN = shape_functions(element_type, xi)
+    grads, jxw = geometry(points, elements, dN, w)          # [E, Q, B, D], [E, Q]
+    dim = points.shape[1]
+    mu = E / (2 * (1 + nu))
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    ue = u[elements]                                        # [E, B, D]
+    gu = np.einsum("ebi,eqbd->eqid", ue, grads)             # [E, Q, D, D]
+    F = np.eye(dim)[None, None] + gu
+    J = np.linalg.det(F)
+    lnJ = np.log(J)
+    I1 = (F * F).sum(axis=(-1, -2))
+    psi = 0.5 * mu * (I1 - dim) - mu * lnJ + 0.5 * lam * lnJ ** 2
+    energy = float((psi * jxw).sum())
+    FinvT = np.swapaxes(np.linalg.inv(F), -1, -2)
+    P = mu * F + (lam * lnJ - mu)[..., None, None] * FinvT  # [E, Q, D, D]
+    fe = np.einsum("eqid,eqbd,eq->ebi", P, grads, jxw)      # [E, B, D]
+    g = np.zeros_like(u, dtype=np.float64)
+    np.add.at(g, elements.reshape(-1), fe.reshape(-1, dim))
+    return energy, g

@@ -12,7 +12,8 @@ from .sparse import SparseMatrix
 from .assemble import (ElementAssembler, NodeAssembler, LaplaceElementAssembler, MassElementAssembler,
                        LinearElasticityElementAssembler, const_node_assembler, func_node_assembler)
 from .condense import Condenser
+from .energy import NeoHookeanModel
 
 __all__ = ["Mesh", "SparseMatrix", "ElementAssembler", "NodeAssembler", "LaplaceElementAssembler",
            "MassElementAssembler", "LinearElasticityElementAssembler", "const_node_assembler",
-           "func_node_assembler", "Condenser"]
+           "func_node_assembler", "Condenser", "NeoHookeanModel"]

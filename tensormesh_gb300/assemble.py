@@ -180,6 +180,29 @@ class ElementAssembler(nn.Module):
         assert isinstance(obj, ElementAssembler), f"obj must be an instance of ElementAssembler, but got {type(obj)}"
         return cls(obj.topology, obj.points, obj.quadrature_order, *args, **kwargs)
 
+    def energy(self, points: Optional[torch.Tensor] = None, func=None, point_data=None, element_data=None,
+               scalar_data=None, batch_size: int = -1):
+        """Total energy sum_e sum_q psi w |det J| (element_assembler.py:468-680).
+
+        Runs on the GPU kernels for the Neo-Hookean density of
+        ``NeoHookeanModel`` with ``point_data={"displacement": u}``; the result
+        is differentiable with respect to u (``.backward()`` leaves the
+        internal force vector in ``u.grad``).  Other densities raise
+        ``NotImplementedError`` (there is no CPU fallback).  ``batch_size`` is
+        accepted and ignored, as for ``__call__``."""
+        from .energy import NeoHookeanModel, neo_hookean_energy
+        density = func if func is not None else getattr(self, "element_energy", None)
+        is_nh = (isinstance(self, NeoHookeanModel) and
+                 getattr(density, "__func__", None) is NeoHookeanModel.element_energy)
+        if not is_nh:
+            raise NotImplementedError("energy assembly on the GPU supports the Neo-Hookean density "
+                                      "(NeoHookeanModel.element_energy)")
+        point_data = dict(point_data or {})
+        point_data.pop("x", None)
+        if set(point_data) != {"displacement"} or element_data or scalar_data:
+            raise NotImplementedError("the Neo-Hookean energy takes point_data={'displacement': u} only")
+        return neo_hookean_energy(self, point_data["displacement"], points, self.mu, self.lam)
+
     @property
     def elements(self):
         return {self.topology.element_type: self.topology.elements}
@@ -429,3 +452,11 @@ def func_node_assembler(f=lambda x: x):
 
     FuncNodeAssembler._builtin_forward = FuncNodeAssembler.forward
     return FuncNodeAssembler
+
+
+def __getattr__(name):
+    # NeoHookeanModel lives in energy.py (it subclasses ElementAssembler)
+    if name == "NeoHookeanModel":
+        from .energy import NeoHookeanModel
+        return NeoHookeanModel
+    raise AttributeError(name)

@@ -110,6 +110,7 @@ def main(ref_root):
     import tensormesh as tm
     from tensormesh.functional.elasticity import voigt_shape_grad, voigt_stiffness
     from tensormesh.sparse.solve.scipy_solve import SparseSolveScipy
+    from tensormesh.assemble import NeoHookeanModel
 
     torch.set_num_threads(max(1, os.cpu_count() or 1))
 
@@ -244,6 +245,20 @@ def main(ref_root):
         "adj/J": np.array(J.item()), "adj/dJ_dkappa": kappa.grad.numpy(), "adj/dJ_dx": x.grad.numpy(),
         "adj/u": u.detach().numpy(),
     })
+    # ------------------------------------ Neo-Hookean energy and its u-gradient
+    rng = np.random.default_rng(13)
+    for etype, (pts, cells, bd) in meshes.items():
+        mesh = mk_mesh(pts, cells, bd, etype)
+        dim = mesh.points.shape[1]
+        u0 = 0.01 * rng.normal(size=(mesh.points.shape[0], dim))
+        out[f"{etype}/nh/u"] = u0
+        for q in (1, 2):
+            model = NeoHookeanModel.from_mesh(mesh, quadrature_order=q, E=2.0, nu=0.3)
+            u = torch.tensor(u0, requires_grad=True)
+            energy = model.energy(u)
+            energy.backward()
+            out[f"{etype}/nh/q{q}/energy"] = np.array(energy.item())
+            out[f"{etype}/nh/q{q}/grad_u"] = u.grad.numpy().copy()
     np.savez_compressed(os.path.join(HERE, "reference_fem.npz"), **out)
     print("wrote", len(out), "arrays")
 

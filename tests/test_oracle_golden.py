@@ -93,3 +93,22 @@ def test_oracle_adjoint_kappa_matches_reference_autograd(golden):
     u = golden["adj/u"]
     g = fem.compliance_gradients_kappa(pts, el, "triangle", 1, kappa, u)
     assert rel_err(g, golden["adj/dJ_dkappa"]) <= 1e-10
+
+
+@pytest.mark.parametrize("etype", ETYPES)
+@pytest.mark.parametrize("q", [1, 2])
+def test_oracle_neo_hookean_matches_reference_energy_and_autograd(golden, etype, q):
+    """NeoHookeanModel.energy(u) and u.grad from the reference's autograd."""
+    pts, el, u = golden[f"{etype}/points"], golden[f"{etype}/elements"], golden[f"{etype}/nh/u"]
+    e, g = fem.neo_hookean(pts, el, etype, q, u, 2.0, 0.3)
+    e_ref = float(golden[f"{etype}/nh/q{q}/energy"])
+    g_ref = golden[f"{etype}/nh/q{q}/grad_u"]
+    assert abs(e - e_ref) <= 1e-12 * abs(e_ref)
+    assert np.max(np.abs(g - g_ref)) <= 1e-12 * np.max(np.abs(g_ref))
+
+
+def test_oracle_neo_hookean_zero_displacement_has_zero_energy(golden):
+    """tests/assemble/test_builtin.py:116-125 of the reference, as an invariant."""
+    pts, el = golden["triangle/points"], golden["triangle/elements"]
+    e, g = fem.neo_hookean(pts, el, "triangle", 2, np.zeros_like(pts), 1.0, 0.3)
+    assert abs(e) <= 1e-14 and np.max(np.abs(g)) <= 1e-14
