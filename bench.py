@@ -305,6 +305,39 @@ def run_ours(args):
                  "elements_per_s": t2.n_elements / (ms_nh * 1e-3), "ms_per_energy_and_gradient": ms_nh}
         del easm, m2, nh
 
+    # ---- C4: gradient of the compliance J = b^T u, K(kappa, x) u = b, with
+    #      respect to the per-element kappa and the nodal coordinates, 256^2
+    #      split square, FP64 (forward assembly + Jacobi-PCG + adjoint solve +
+    #      backward assembly)
+    adjoint = None
+    if not args.no_extra:
+        m4 = tg.Mesh.gen_unit_square(256, device=dev)
+        k4 = torch.from_numpy(np.exp(np.random.default_rng(SEED + 4).normal(size=m4.n_elements))).to(dev)
+        a4 = KappaLaplace.from_mesh(m4, quadrature_order=1)
+        l4 = tg.const_node_assembler(1.0).from_mesh(m4, quadrature_order=1)
+        c4 = tg.Condenser(m4.boundary_mask)
+
+        def c4_step():
+            x = m4.points.clone().requires_grad_(True)
+            kk = k4.clone().requires_grad_(True)
+            K4 = a4(x, element_data={"kappa": kk})
+            b4 = l4(x)
+            K_ii4, f_i4 = c4(K4, b4)
+            u4 = c4.recover(K_ii4.solve(f_i4, rtol=1e-10))
+            (b4 * u4).sum().backward()
+            return K_ii4.last_solve_info.iterations
+        c4_step()
+        torch.cuda.synchronize()
+        ta4 = time.perf_counter()
+        its4 = c4_step()
+        torch.cuda.synchronize()
+        adjoint = {"workload": "256^2 split unit square, P1, kappa = exp(N(0,1)) per element, FP64: dJ/dkappa and "
+                               "dJ/dx of J = b^T u (forward assembly, Jacobi-PCG to 1e-10, adjoint solve, "
+                               "backward assembly)",
+                   "elements": m4.n_elements, "seconds_per_gradient": time.perf_counter() - ta4,
+                   "pcg_iterations_forward": its4}
+        del a4, l4, c4, m4
+
     # ---- C3: 256 uneven 2D Poisson meshes, assembled + Jacobi-PCG in one
     #      persistent, graph-captured launch (FP32), autotuned launch shape
     batched = None
@@ -470,6 +503,7 @@ def run_ours(args):
             "fp32_variant": fp32,
             "elasticity_c2": elast,
             "neo_hookean_energy": hyper,
+            "adjoint_c4": adjoint,
             "batched_c3": batched,
             "gpu_launches": args.steps,
             "clocks": clk,
