@@ -317,26 +317,33 @@ def run_ours(args):
         l4 = tg.const_node_assembler(1.0).from_mesh(m4, quadrature_order=1)
         c4 = tg.Condenser(m4.boundary_mask)
 
-        def c4_step():
+        from tensormesh_gb300.learned import LearnedPreconditioner
+        two4 = LearnedPreconditioner(None, coarse_target=256, use_network=False,
+                                     coords=m4.points[~m4.boundary_mask].contiguous())
+
+        def c4_step(pre):
             x = m4.points.clone().requires_grad_(True)
             kk = k4.clone().requires_grad_(True)
             K4 = a4(x, element_data={"kappa": kk})
             b4 = l4(x)
             K_ii4, f_i4 = c4(K4, b4)
-            u4 = c4.recover(K_ii4.solve(f_i4, rtol=1e-10))
+            kw = {} if pre is None else {"preconditioner": pre}
+            u4 = c4.recover(K_ii4.solve(f_i4, rtol=1e-10, **kw))
             (b4 * u4).sum().backward()
             return K_ii4.last_solve_info.iterations
-        c4_step()
-        torch.cuda.synchronize()
-        ta4 = time.perf_counter()
-        its4 = c4_step()
-        torch.cuda.synchronize()
+        res4 = {}
+        for name, pre in (("jacobi_pcg", None), ("two_level_pcg", two4)):
+            c4_step(pre)
+            torch.cuda.synchronize()
+            ta4 = time.perf_counter()
+            its4 = c4_step(pre)
+            torch.cuda.synchronize()
+            res4[name] = {"seconds_per_gradient": time.perf_counter() - ta4, "iterations_forward_solve": its4}
         adjoint = {"workload": "256^2 split unit square, P1, kappa = exp(N(0,1)) per element, FP64: dJ/dkappa and "
-                               "dJ/dx of J = b^T u (forward assembly, Jacobi-PCG to 1e-10, adjoint solve, "
+                               "dJ/dx of J = b^T u (forward assembly, PCG to 1e-10, adjoint solve, "
                                "backward assembly)",
-                   "elements": m4.n_elements, "seconds_per_gradient": time.perf_counter() - ta4,
-                   "pcg_iterations_forward": its4}
-        del a4, l4, c4, m4
+                   "elements": m4.n_elements, **res4}
+        del a4, l4, c4, m4, two4
 
     # ---- C3: 256 uneven 2D Poisson meshes, assembled + Jacobi-PCG in one
     #      persistent, graph-captured launch (FP32), autotuned launch shape

@@ -259,10 +259,11 @@ class LearnedPreconditioner:
     thin K P.  ``use_network=False`` gives the same method with w = 1."""
 
     def __init__(self, model: Optional[MPNN] = None, device="cuda", coarse_target: int = 512,
-                 use_network: bool = True):
+                 use_network: bool = True, coords: Optional[torch.Tensor] = None):
         self.model = model or MPNN(device)
         self.coarse_target = coarse_target
         self.use_network = use_network
+        self.coords = coords          # dof coordinates, used when solve() gets none
         self._setup_key = None
 
     def setup(self, A, coords):
@@ -365,6 +366,8 @@ class LearnedPreconditioner:
         """Flexible CG (Polak-Ribiere beta) with this preconditioner; falls
         back to Jacobi-PCG if the residual stagnates (``fallback=False``
         returns after ``maxiter`` iterations instead).  x is updated in place."""
+        if coords is None:
+            coords = self.coords
         if coords is None:
             raise ValueError("the learned preconditioner needs dof coordinates (coords=) for its coarse space")
         t0 = time.perf_counter()

@@ -130,3 +130,31 @@ def test_training_and_two_level_solve_against_jacobi_pcg():
                                                                                        coords=coords)
         assert info.status == 0 and info.residual <= 1e-8 and not info.fallback
         assert info.iterations < jac_its, (use, info.iterations, jac_its)
+
+
+def test_solve_hook_and_adjoint_with_two_level_preconditioner():
+    """K.solve(..., preconditioner=pre) in the forward and the adjoint solve:
+    the compliance and its kappa-gradient agree with the Jacobi-PCG ones."""
+    mesh = tg.Mesh.gen_unit_square(48, device=DEV)
+    g = torch.Generator().manual_seed(4)
+    kappa0 = torch.exp(torch.randn(mesh.n_elements, generator=g, dtype=torch.float64)).to(DEV)
+
+    class KL(tg.ElementAssembler):
+        def forward(self, gradu, gradv, kappa):
+            return kappa * (gradu @ gradv)
+    asm = KL.from_mesh(mesh, quadrature_order=1)
+    load = tg.const_node_assembler(1.0).from_mesh(mesh, quadrature_order=1)
+    cond = tg.Condenser(mesh.boundary_mask)
+    pre = LearnedPreconditioner(None, coarse_target=64, use_network=False,
+                                coords=mesh.points[~mesh.boundary_mask].contiguous())
+    out = []
+    for kw in ({}, {"preconditioner": pre}):
+        kappa = kappa0.clone().requires_grad_(True)
+        K = asm(mesh.points, element_data={"kappa": kappa})
+        b = load(mesh.points)
+        K_ii, f_i = cond(K, b)
+        J = (b * cond.recover(K_ii.solve(f_i, rtol=1e-12, **kw))).sum()
+        J.backward()
+        out.append((float(J.detach()), kappa.grad.clone()))
+    assert abs(out[0][0] - out[1][0]) <= 1e-10 * abs(out[0][0])
+    assert float((out[0][1] - out[1][1]).abs().max()) <= 1e-8 * float(out[0][1].abs().max())
