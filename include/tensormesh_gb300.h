@@ -117,6 +117,8 @@ typedef struct tm_patch_plan {
   const uint64_t* inc_pack;   /* P1 tetrahedra (NULL otherwise) */
   const uint32_t* inc_pack32; /* NULL when it does not fit */
   const uint8_t* rdiag;       /* with inc_pack */
+  int32_t max_deg;            /* max entries of one CSR row */
+  int32_t pad1;
 } tm_patch_plan;
 
 typedef struct tm_assemble_args {

@@ -52,6 +52,7 @@ class PatchPlan(ctypes.Structure):
         ("max_vtx", ctypes.c_int32), ("max_slots", ctypes.c_int32),
         ("max_rows", ctypes.c_int32), ("max_elems", ctypes.c_int32),
         ("inc_pack", P), ("inc_pack32", P), ("rdiag", P),
+        ("max_deg", ctypes.c_int32), ("pad1", ctypes.c_int32),
     ]
 
 

@@ -108,33 +108,35 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
   const int rbeg = plan.rptr[p], nr = plan.rptr[p + 1] - rbeg;
   if (nr == 0) return;
 
+  // Accumulators are column-major over the patch's rows: entry k of local row
+  // lr sits at s_acc[k * nrp + lr], nrp = max_rows rounded up to 16, so the
+  // 16 lanes of a half-warp (consecutive rows) hit 16 distinct bank pairs
+  // whatever columns their incidences touch.
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  int64_t* s_out0 = reinterpret_cast<int64_t*>(smem_raw);         // [kThreads] CSR offset of each row
-  uint32_t* s_rd = reinterpret_cast<uint32_t*>(s_out0 + kThreads); // [kThreads] acc offset | degree << 24
-  S* s_X = reinterpret_cast<S*>(s_rd + kThreads);                  // [max_vtx][3]
+  const int nrp = (plan.max_rows + 15) & ~15;
+  S* s_X = reinterpret_cast<S*>(smem_raw);                         // [max_vtx][3]
   S* s_pc = s_X + plan.max_vtx * 3;                                // [max_vtx] point coef
   const int pc_len = args.coef_kind == TM_COEF_POINT ? plan.max_vtx : 0;
-  S* s_acc = s_pc + pc_len;                                        // [max_slots]
-  S* s_stage = s_acc + plan.max_slots;                             // [10][chunk]
+  S* s_acc = s_pc + pc_len;                                        // [max_deg][nrp]
+  S* s_stage = s_acc + plan.max_deg * nrp;                         // [10][chunk]
 
   // ---- phase 0: row state (the launcher guarantees nr <= kThreads, so a
   // thread owns at most one row; its incidence cursor and the next packed
   // record stay in registers across chunks), coordinates, coefficients
   const bool owner = tid < nr;
-  int cur = 0, end = 0, ro = 0, dpos = 0;
+  int cur = 0, end = 0, dpos = 0, deg = 0;
+  int64_t o0 = 0;
   RW rec = R::kEnd;
+  S* acc = s_acc + tid;  // this thread's row: entry k at acc[k * nrp]
   if (owner) {
     const int r = plan.rows[rbeg + tid];
-    const int64_t o0 = plan.indptr[r];
-    const int deg = (int)(plan.indptr[r + 1] - o0);
-    ro = plan.racc[rbeg + tid];
+    o0 = plan.indptr[r];
+    deg = (int)(plan.indptr[r + 1] - o0);
     dpos = plan.rdiag[rbeg + tid];
     cur = plan.iptr[rbeg + tid];
     end = plan.iptr[rbeg + tid + 1];
     if (cur < end) rec = recs[cur];
-    s_out0[tid] = o0;
-    s_rd[tid] = (uint32_t)ro | ((uint32_t)deg << 24);
-    for (int k = 0; k < deg; ++k) s_acc[ro + k] = P::st(P::zero());
+    for (int k = 0; k < deg; ++k) acc[k * nrp] = P::st(P::zero());
   }
   const T* pts = static_cast<const T*>(args.points);
   for (int i = tid; i < nv * 3; i += kThreads) {
@@ -239,49 +241,43 @@ p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) 
         const uint32_t u = (uint32_t)(kTet4Stage >> (16 * a));
         dg = P::add(dg, P::ld(s_stage[(int)(u & 15u) * chunk + lo]));
         int pos[3];
-        S v[3], acc[3];
+        S v[3], old[3];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          pos[j] = ro + R::pos(rec, j);
+          pos[j] = R::pos(rec, j) * nrp;
           v[j] = s_stage[(int)((u >> (4 * j + 4)) & 15u) * chunk + lo];
         }
 #pragma unroll
-        for (int j = 0; j < 3; ++j) acc[j] = s_acc[pos[j]];
+        for (int j = 0; j < 3; ++j) old[j] = acc[pos[j]];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) s_acc[pos[j]] = P::st(P::add(P::ld(acc[j]), P::ld(v[j])));
+        for (int j = 0; j < 3; ++j) acc[pos[j]] = P::st(P::add(P::ld(old[j]), P::ld(v[j])));
         any = true;
         rec = next;
         ++cur;
       }
-      if (any) s_acc[ro + dpos] = P::st(P::add(P::ld(s_acc[ro + dpos]), dg));
+      if (any) acc[dpos * nrp] = P::st(P::add(P::ld(acc[dpos * nrp]), dg));
     }
     __syncthreads();
   }
-  // --- write the finished rows: half a warp per row, row metadata from shared
-  T* out = static_cast<T*>(args.out);
-  const int hl = tid & 15;
-#pragma unroll 1
-  for (int lr = tid >> 4; lr < nr; lr += kThreads / 16) {
-    const int64_t o0 = s_out0[lr];
-    const uint32_t rd = s_rd[lr];
-    const int r0 = (int)(rd & 0xffffffu), deg = (int)(rd >> 24);
-#pragma unroll 1
-    for (int k = hl; k < deg; k += 16) out[o0 + k] = (T)P::out(s_acc[r0 + k]);
+  // --- write the finished row: only its owner ever touched it, so no barrier
+  // is needed; consecutive lanes write consecutive rows' k-th entries
+  if (owner) {
+    T* out = static_cast<T*>(args.out);
+    for (int k = 0; k < deg; ++k) out[o0 + k] = (T)P::out(acc[k * nrp]);
   }
 }
 
 inline size_t p1tet_smem_bytes(const tm_patch_plan& plan, int coef_kind, int chunk, size_t elem = sizeof(float2)) {
-  size_t n2 = (size_t)plan.max_vtx * 3 + (coef_kind == TM_COEF_POINT ? plan.max_vtx : 0) + plan.max_slots +
-              (size_t)10 * chunk;
-  return (size_t)kThreads * (sizeof(int64_t) + sizeof(uint32_t)) + n2 * elem + 64;
+  const size_t nrp = (size_t)((plan.max_rows + 15) & ~15);
+  size_t n2 = (size_t)plan.max_vtx * 3 + (coef_kind == TM_COEF_POINT ? plan.max_vtx : 0) +
+              (size_t)plan.max_deg * nrp + (size_t)10 * chunk;
+  return n2 * elem + 64;
 }
 
 // The fast path needs every patch to own at most kThreads rows (one row per
-// thread) and fewer than 2^24 accumulator slots; other plans take the generic
-// patch kernel.
+// thread); other plans take the generic patch kernel.
 inline bool p1tet_fast_ok(const tm_patch_plan& plan) {
-  return plan.inc_pack != nullptr && plan.rdiag != nullptr && plan.max_rows <= kThreads &&
-         plan.max_slots < (1 << 24);
+  return plan.inc_pack != nullptr && plan.rdiag != nullptr && plan.max_rows <= kThreads && plan.max_deg > 0;
 }
 
 template <class T, class A, class RW>

@@ -352,6 +352,7 @@ class PatchPlan:
         self.max_slots = int(slots_per_part.max()) if N else 0
         self.max_rows = int(rows_per_part.max()) if N else 0
         self.max_elems = int(elems_per_part.max()) if E else 0
+        self.max_deg = int(deg.max()) if N else 0
         self.n_pairs = int(pairs.shape[0])
         self.n_incidences = int(pi.shape[0])
         if int(iptr[-1]) >= 2**31 or self.n_pairs * B >= 2**31:
@@ -372,6 +373,7 @@ class PatchPlan:
         s.inc_pack32 = 0 if self.inc_pack32 is None else self.inc_pack32.data_ptr()
         s.rdiag = 0 if self.rdiag is None else self.rdiag.data_ptr()
         s.max_vtx, s.max_slots, s.max_rows, s.max_elems = self.max_vtx, self.max_slots, self.max_rows, self.max_elems
+        s.max_deg, s.pad1 = self.max_deg, 0
         return s
 
     def nbytes(self) -> int:
