@@ -201,7 +201,7 @@ def run_ours(args):
         asm.slot_budget, tuned = args.slot_budget, {"table": []}
     else:
         tuned = asm.autotune(mesh.points, element_data={"kappa": kappa}, use_cache=False,
-                             budgets=(512, 1024, 2048, 4096, 6144))
+                             budgets=(512, 1024, 2048, 3072, 4096, 6144))
     topo = asm.topology
     E, N, B, D = topo.n_elements, topo.n_points, topo.n_basis, topo.dim
     nnz = topo.pattern.nnz
@@ -261,7 +261,7 @@ def run_ours(args):
         kap32 = kappa.float()
         asm32 = KappaLaplace.from_assembler(asm)
         tuned32 = asm32.autotune(pts32, element_data={"kappa": kap32}, use_cache=False,
-                                 budgets=(512, 1024, 2048, 4096, 6144))
+                                 budgets=(512, 1024, 2048, 3072, 4096, 6144))
         ms32 = time_calls(lambda: asm32(pts32, element_data={"kappa": kap32}))
         alg32 = algorithmic_bytes(E, B, D, N, nnz, itemsize=4)
         fp32 = {"elements_per_s": E / (ms32 * 1e-3), "kernel_ms": ms32, "algorithmic_bytes": alg32,
