@@ -19,7 +19,9 @@
 namespace tmg {
 
 constexpr int kPcgThreads = 512;
-constexpr int kGroup = 8;  // lanes per CSR row
+constexpr int kGroup = 8;  // lanes per CSR row (float32 kernel, first residual)
+constexpr int kDfRows = 2; // rows a thread advances together (double-float iteration)
+constexpr int kDfIlp = 4;  // CSR entries of each row fetched per round
 
 struct PcgState {
   unsigned int count;
@@ -239,7 +241,7 @@ __global__ void split_kernel(int64_t n, const double* __restrict__ src, F2* __re
   }
 }
 
-__global__ void __launch_bounds__(kPcgThreads)
+__global__ void __launch_bounds__(kPcgThreads, 2)
 pcg_df64_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ idx,
                 const F2* __restrict__ val, const double* __restrict__ bd, double* __restrict__ xd, F2* x, F2* r,
                 F2* z, F2* p0, F2* p1, F2* q, F2* dinv, double* partials, PcgState* st, double rtol, double atol,
@@ -326,24 +328,50 @@ pcg_df64_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __
     }
     if (it == maxiter) break;
     df64 pq_l = zero;
-    for (int64_t base = r0; base < r1; base += ngroups) {
-      const int64_t row = base + g;
-      const bool valid = row < r1;
-      df64 s = zero;
-      if (valid)
-        for (int64_t k = indptr[row] + lane; k < indptr[row + 1]; k += kGroup) {
-          const int c = idx[k];
-          s += ld2(val, k) * (ld2(z, c) + beta * ld2(pold, c));
-        }
+    // one thread per row, kDfRows rows at a time, kDfIlp entries of each row
+    // per round with every load of the round issued before the first use
+    // (the gathers of a round are independent, so they overlap in flight)
+    for (int64_t base = r0 + threadIdx.x; base < r1; base += kDfRows * kPcgThreads) {
+      int64_t k0[kDfRows], k1[kDfRows];
+      df64 s[kDfRows];
 #pragma unroll
-      for (int o = kGroup / 2; o > 0; o >>= 1) {
-        df64 tt{__shfl_down_sync(0xffffffffu, s.hi, o, kGroup), __shfl_down_sync(0xffffffffu, s.lo, o, kGroup)};
-        s += tt;
+      for (int u = 0; u < kDfRows; ++u) {
+        const int64_t row = base + (int64_t)u * kPcgThreads;
+        const bool ok = row < r1;
+        k0[u] = ok ? indptr[row] : 0;
+        k1[u] = ok ? indptr[row + 1] : 0;
+        s[u] = zero;
       }
-      if (valid && lane == 0) {
-        const df64 pv = ld2(z, row) + beta * ld2(pold, row);
-        st2(q, row, s);
-        pq_l += pv * s;
+      for (int64_t j0 = 0;; j0 += kDfIlp) {
+        bool more = false;
+#pragma unroll
+        for (int u = 0; u < kDfRows; ++u) more |= k0[u] + j0 < k1[u];
+        if (!more) break;
+        int c[kDfRows][kDfIlp];
+        F2 v[kDfRows][kDfIlp];
+#pragma unroll
+        for (int u = 0; u < kDfRows; ++u)
+#pragma unroll
+          for (int j = 0; j < kDfIlp; ++j) {
+            const int64_t kk = k0[u] + j0 + j;
+            const bool ok = kk < k1[u];
+            c[u][j] = ok ? idx[kk] : 0;
+            v[u][j] = ok ? val[kk] : F2{0.f, 0.f};
+          }
+#pragma unroll
+        for (int u = 0; u < kDfRows; ++u)
+#pragma unroll
+          for (int j = 0; j < kDfIlp; ++j)
+            s[u] += df64{v[u][j].hi, v[u][j].lo} * (ld2(z, c[u][j]) + beta * ld2(pold, c[u][j]));
+      }
+#pragma unroll
+      for (int u = 0; u < kDfRows; ++u) {
+        const int64_t row = base + (int64_t)u * kPcgThreads;
+        if (row < r1) {
+          const df64 pv = ld2(z, row) + beta * ld2(pold, row);
+          st2(q, row, s[u]);
+          pq_l += pv * s[u];
+        }
       }
     }
     t = block_sum(tm_to_double(pq_l), s_red);
@@ -356,16 +384,37 @@ pcg_df64_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __
     }
     const df64 alpha = tm_from_double(rz / pq);
     df64 rz_n = zero, rr_n = zero;
-    for (int64_t row = r0 + threadIdx.x; row < r1; row += kPcgThreads) {
-      const df64 pv = ld2(z, row) + beta * ld2(pold, row);
-      st2(pnew, row, pv);
-      st2(x, row, ld2(x, row) + alpha * pv);
-      const df64 rv = ld2(r, row) - alpha * ld2(q, row);
-      st2(r, row, rv);
-      const df64 zv = ld2(dinv, row) * rv;
-      st2(z, row, zv);
-      rz_n += rv * zv;
-      rr_n += rv * rv;
+    // kDfRows rows per round, all loads before any store (the vectors are
+    // distinct arrays, which the compiler cannot prove)
+    for (int64_t base = r0 + threadIdx.x; base < r1; base += kDfRows * kPcgThreads) {
+      F2 zz[kDfRows], po[kDfRows], xx[kDfRows], rr_[kDfRows], qq[kDfRows], di[kDfRows];
+#pragma unroll
+      for (int u = 0; u < kDfRows; ++u) {
+        const int64_t row = base + (int64_t)u * kPcgThreads;
+        const bool ok = row < r1;
+        const F2 zf{0.f, 0.f};
+        zz[u] = ok ? z[row] : zf;
+        po[u] = ok ? pold[row] : zf;
+        xx[u] = ok ? x[row] : zf;
+        rr_[u] = ok ? r[row] : zf;
+        qq[u] = ok ? q[row] : zf;
+        di[u] = ok ? dinv[row] : zf;
+      }
+#pragma unroll
+      for (int u = 0; u < kDfRows; ++u) {
+        const int64_t row = base + (int64_t)u * kPcgThreads;
+        if (row < r1) {
+          const df64 pv = df64{zz[u].hi, zz[u].lo} + beta * df64{po[u].hi, po[u].lo};
+          const df64 rv = df64{rr_[u].hi, rr_[u].lo} - alpha * df64{qq[u].hi, qq[u].lo};
+          const df64 zv = df64{di[u].hi, di[u].lo} * rv;
+          st2(pnew, row, pv);
+          st2(x, row, df64{xx[u].hi, xx[u].lo} + alpha * pv);
+          st2(r, row, rv);
+          st2(z, row, zv);
+          rz_n += rv * zv;
+          rr_n += rv * rv;
+        }
+      }
     }
     t = block_sum(tm_to_double(rz_n), s_red);
     if (threadIdx.x == 0) partB[blockIdx.x] = t;
