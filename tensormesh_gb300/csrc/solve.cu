@@ -159,23 +159,50 @@ pcg_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restr
       break;
     }
     if (it == maxiter) break;
-    // q = A p_new, p_new = z + beta p_old formed on the fly; partial p.q
+    // q = A p_new, p_new = z + beta p_old formed on the fly; partial p.q.
+    // One thread per row, kDfRows rows and kDfIlp entries per round with all
+    // loads of the round issued before the first use.
     T pq_l = 0;
-    for (int64_t base = r0; base < r1; base += ngroups) {
-      const int64_t row = base + g;
-      const bool valid = row < r1;
-      T s = 0;
-      if (valid)
-        for (int64_t k = indptr[row] + lane; k < indptr[row + 1]; k += kGroup) {
-          const int c = idx[k];
-          s += val[k] * (z[c] + beta * pold[c]);
-        }
+    for (int64_t base = r0 + threadIdx.x; base < r1; base += kDfRows * kPcgThreads) {
+      int64_t k0[kDfRows], k1[kDfRows];
+      T s[kDfRows];
 #pragma unroll
-      for (int o = kGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kGroup);
-      if (valid && lane == 0) {
-        T pv = z[row] + beta * pold[row];
-        q[row] = s;
-        pq_l += pv * s;
+      for (int u = 0; u < kDfRows; ++u) {
+        const int64_t row = base + (int64_t)u * kPcgThreads;
+        const bool ok = row < r1;
+        k0[u] = ok ? indptr[row] : 0;
+        k1[u] = ok ? indptr[row + 1] : 0;
+        s[u] = 0;
+      }
+      for (int64_t j0 = 0;; j0 += kDfIlp) {
+        bool more = false;
+#pragma unroll
+        for (int u = 0; u < kDfRows; ++u) more |= k0[u] + j0 < k1[u];
+        if (!more) break;
+        int c[kDfRows][kDfIlp];
+        T v[kDfRows][kDfIlp];
+#pragma unroll
+        for (int u = 0; u < kDfRows; ++u)
+#pragma unroll
+          for (int j = 0; j < kDfIlp; ++j) {
+            const int64_t kk = k0[u] + j0 + j;
+            const bool ok = kk < k1[u];
+            c[u][j] = ok ? idx[kk] : 0;
+            v[u][j] = ok ? val[kk] : T(0);
+          }
+#pragma unroll
+        for (int u = 0; u < kDfRows; ++u)
+#pragma unroll
+          for (int j = 0; j < kDfIlp; ++j) s[u] += v[u][j] * (z[c[u][j]] + beta * pold[c[u][j]]);
+      }
+#pragma unroll
+      for (int u = 0; u < kDfRows; ++u) {
+        const int64_t row = base + (int64_t)u * kPcgThreads;
+        if (row < r1) {
+          const T pv = z[row] + beta * pold[row];
+          q[row] = s[u];
+          pq_l += pv * s[u];
+        }
       }
     }
     t = block_sum(pq_l, s_red);
@@ -189,17 +216,36 @@ pcg_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restr
     const T alpha = rz / pq;
     T rz_n = 0, rr_n = 0;
     // every row of p_new is written here by its owner (rows were read as
-    // z + beta*pold above, which this CTA's rows still hold in z/pold)
-    for (int64_t row = r0 + threadIdx.x; row < r1; row += kPcgThreads) {
-      T pv = z[row] + beta * pold[row];
-      pnew[row] = pv;
-      x[row] += alpha * pv;
-      T rv = r[row] - alpha * q[row];
-      r[row] = rv;
-      T zv = dinv[row] * rv;
-      z[row] = zv;
-      rz_n += rv * zv;
-      rr_n += rv * rv;
+    // z + beta*pold above, which this CTA's rows still hold in z/pold);
+    // kDfRows rows per round, all loads before any store
+    for (int64_t base = r0 + threadIdx.x; base < r1; base += kDfRows * kPcgThreads) {
+      T zz[kDfRows], po[kDfRows], xx[kDfRows], rr_[kDfRows], qq[kDfRows], di[kDfRows];
+#pragma unroll
+      for (int u = 0; u < kDfRows; ++u) {
+        const int64_t row = base + (int64_t)u * kPcgThreads;
+        const bool ok = row < r1;
+        zz[u] = ok ? z[row] : T(0);
+        po[u] = ok ? pold[row] : T(0);
+        xx[u] = ok ? x[row] : T(0);
+        rr_[u] = ok ? r[row] : T(0);
+        qq[u] = ok ? q[row] : T(0);
+        di[u] = ok ? dinv[row] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < kDfRows; ++u) {
+        const int64_t row = base + (int64_t)u * kPcgThreads;
+        if (row < r1) {
+          const T pv = zz[u] + beta * po[u];
+          const T rv = rr_[u] - alpha * qq[u];
+          const T zv = di[u] * rv;
+          pnew[row] = pv;
+          x[row] = xx[u] + alpha * pv;
+          r[row] = rv;
+          z[row] = zv;
+          rz_n += rv * zv;
+          rr_n += rv * rv;
+        }
+      }
     }
     t = block_sum(rz_n, s_red);
     if (threadIdx.x == 0) partB[blockIdx.x] = t;
