@@ -232,7 +232,8 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_assemble_pcg_kernel(
       }
       t0 = cta_sum(pq_l, red);
       if (threadIdx.x == 0) part[par][0] = t0;
-      __threadfence();
+      // the cluster barrier's arrive/wait carry release/acquire semantics at
+      // cluster scope: the q rows written above are visible to the other CTAs
       cl.sync();
       const double pq = cluster_combine(cl, &part[par][0]);
       if (!(pq > 0.0)) {
@@ -278,7 +279,6 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_assemble_pcg_kernel(
         part[par][1] = rz_n;
         part[par][2] = rr_n;
       }
-      __threadfence();
       cl.sync();
       const double rzn = cluster_combine(cl, &part[par][1]);
       rr = cluster_combine(cl, &part[par][2]);

@@ -147,3 +147,28 @@ def test_packed_tet_records_reproduce_oracle(budget):
     for bits32 in (False, True):
         got = replay_packed(plan, Ke, ix.shape[0], bits32)
         assert np.max(np.abs(got - dv)) <= 1e-13 * np.max(np.abs(dv))
+
+
+def test_rcb_partition_any_number_of_parts_is_balanced():
+    from tensormesh_gb300.plan import rcb_partition
+    g = torch.Generator().manual_seed(0)
+    c = torch.rand(20000, 3, generator=g, dtype=torch.float64)
+    for P in (1, 3, 7, 64, 391):
+        part = rcb_partition(c, n_parts=P)
+        cnt = torch.bincount(part, minlength=P)
+        assert int(part.max()) + 1 == P
+        assert int(cnt.max()) - int(cnt.min()) <= 1
+
+
+def test_morton_parts_are_octree_cells():
+    from tensormesh_gb300.plan import morton_parts
+    i = torch.arange(1, 32, dtype=torch.float64) / 32
+    pts = torch.stack(torch.meshgrid(i, i, i, indexing="ij"), -1).reshape(-1, 3)
+    part = morton_parts(pts, 64)
+    cnt = torch.bincount(part)
+    assert int(cnt.max()) <= 2 * 64 and int(part.max()) + 1 == cnt.shape[0]
+    # every part is an axis-aligned box of grid points (a cell of the octree)
+    for k in range(0, int(part.max()) + 1, 37):
+        sel = pts[part == k] * 32
+        ext = (sel.max(0).values - sel.min(0).values + 1).round().long()
+        assert int(ext.prod()) == sel.shape[0]
