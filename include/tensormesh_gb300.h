@@ -186,7 +186,7 @@ int tm_segment_sum(int32_t dtype, int64_t n_segments, const int64_t* ptr, const 
  * ||r|| <= rtol ||b||, writing x and per-instance status / iterations /
  * residual.  work: 6 * n_rows floats.  queue: one device uint.
  * Replaces the reference's per-mesh Python loop of assembler calls and
- * solves (no batched path exists in the reference; SURVEY C3).
+ * solves (no batched path exists in the reference).
  */
 typedef struct tm_batched_args {
   int32_t element;     /* TM_TRI3 or TM_TET4 */

@@ -5,7 +5,7 @@ and the deterministic segmented reductions (``tm_segment_sum``).
 Gradients are returned for the nodal coordinates and for the integrand's
 coefficient (element data, point data or values at quadrature points), the
 two inputs the reference differentiates through its autograd chain
-(SURVEY of TensorMesh: element/element.py:962-966 Jacobian/inverse,
+(element/element.py:962-966 Jacobian/inverse,
 element/transformation.py:1289 JxW, assemble/projector.py:125 scatter).
 """
 from __future__ import annotations

@@ -3,7 +3,7 @@ graph-captured launch, with an autotuner for its launch shape.
 
 The reference has no batched path: a user loops over meshes in Python,
 calling ``Assembler.from_mesh(mesh)(...)``, ``Condenser`` and ``K.solve``
-once per mesh (SURVEY of TensorMesh, config C3).  ``BatchedPoisson`` takes the
+once per mesh.  ``BatchedPoisson`` takes the
 list of meshes once, builds a union patch plan whose patches never straddle
 instances, and then every call
 

@@ -2,7 +2,7 @@
 // the nodal coordinates and the integrand coefficient, given dL/d(values).
 //
 // The reference obtains these by autograd through its vmap/einsum chain,
-// torch.inverse and the index_add_ scatter (SURVEY: element/element.py:
+// torch.inverse and the index_add_ scatter (element/element.py:
 // 962-966, element/transformation.py:1289, assemble/projector.py:125).  Here
 // one hand-written kernel runs the chain rule per element.  With
 // P = dN J^-T (physical gradients), |det J| and the quadrature weight w,

@@ -1,6 +1,6 @@
 """Learned preconditioner: a mesh-graph message-passing network (MPNN) sets
 the smoother of a two-level preconditioner used inside flexible PCG, with
-Jacobi-PCG as fallback and judge.
+Jacobi-PCG as fallback; the true residual decides convergence.
 
 Network (hidden width 64, BF16 weights and activations on the tensor cores,
 FP32 accumulation -- kernels in csrc/mpnn.cu):
