@@ -270,7 +270,7 @@ def run_ours(args):
         if os.path.exists(peaks_path_):
             fp32["hbm_frac"] = fp32["achieved_gbs"] / float(json.load(open(peaks_path_))["hbm_gbs"])
 
-    # ---- C2: 64^3 P1-tet linear elasticity, per-element E, FP64 (secondary)
+    # ---- 64^3 P1-tet linear elasticity, per-element E, FP64 (secondary)
     elast = None
     hyper = None
     if not args.no_extra:
@@ -305,7 +305,7 @@ def run_ours(args):
                  "elements_per_s": t2.n_elements / (ms_nh * 1e-3), "ms_per_energy_and_gradient": ms_nh}
         del easm, m2, nh
 
-    # ---- C4: gradient of the compliance J = b^T u, K(kappa, x) u = b, with
+    # ---- gradient of the compliance J = b^T u, K(kappa, x) u = b, with
     #      respect to the per-element kappa and the nodal coordinates, 256^2
     #      split square, FP64 (forward assembly + Jacobi-PCG + adjoint solve +
     #      backward assembly)
@@ -345,7 +345,7 @@ def run_ours(args):
                    "elements": m4.n_elements, **res4}
         del a4, l4, c4, m4, two4
 
-    # ---- C3: 256 uneven 2D Poisson meshes, assembled + Jacobi-PCG in one
+    # ---- 256 uneven 2D Poisson meshes, assembled + Jacobi-PCG in one
     #      persistent, graph-captured launch (FP32), autotuned launch shape
     batched = None
     if not args.no_extra:
@@ -510,10 +510,10 @@ def run_ours(args):
                     "pipelining": "consecutive steps on two alternating streams"},
             "cpu_baseline": cpu,
             "fp32_variant": fp32,
-            "elasticity_c2": elast,
+            "elasticity_64cube": elast,
             "neo_hookean_energy": hyper,
-            "adjoint_c4": adjoint,
-            "batched_c3": batched,
+            "adjoint_256_square": adjoint,
+            "batched_256_meshes": batched,
             "gpu_launches": args.steps,
             "clocks": clk,
             "pcg": pcg,

@@ -1,5 +1,5 @@
 // Specialised path for isotropic linear elasticity on P1 tetrahedra (FP64
-// emulated or FP32), the C2 case: same patch decomposition and fixed-order
+// emulated or FP32): same patch decomposition and fixed-order
 // row-owner accumulation as the generic kernel, with the element algebra in
 // closed form.
 //

@@ -203,7 +203,7 @@ def main(ref_root):
         asm = tm.LaplaceElementAssembler.from_mesh(mesh, quadrature_order=1)
         out[f"{etype}/ref_edges"] = asm.edges.numpy().astype(np.int64)
 
-    # -------------------------------------------------- C1 Poisson, 64 x 64
+    # -------------------------------------------------- Poisson on the 64 x 64 square
     pts, cells, bd = square_mesh(64)
     mesh = mk_mesh(pts, cells, bd, "triangle")
     K = tm.LaplaceElementAssembler.from_mesh(mesh, quadrature_order=1)(mesh.points)

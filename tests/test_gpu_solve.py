@@ -1,5 +1,5 @@
 """SpMV, Condenser and Jacobi-PCG on the GPU against the reference pipeline
-(golden C1: 64x64 Poisson, reference assembler + Condenser + scipy direct
+(golden: 64x64 Poisson, reference assembler + Condenser + scipy direct
 solve) and the oracle."""
 import math
 
