@@ -169,3 +169,34 @@ def test_cpu_tensors_fail_loudly():
     mesh = tg.Mesh.gen_unit_square(4)
     with pytest.raises(RuntimeError):
         tg.LaplaceElementAssembler.from_mesh(mesh)(mesh.points)
+
+
+@pytest.mark.parametrize("ring", [40, 250])
+def test_high_valence_rows_match_oracle(ring):
+    """A bipyramid fan of tetrahedra: both apexes touch every ring node, so
+    their rows hold ring + 2 entries.  40 exceeds the 32-bit incidence record
+    (64-bit records in the P1-tet kernel); 250 exceeds that kernel's shared
+    memory (the generic kernel takes the launch).  The 250-fan's elements are
+    slivers (ring edge 0.025 against height 1): the element algebra amplifies
+    rounding by about the squared aspect ratio, so double-float (2^-48) meets
+    1e-10 there, float32 1e-3, and the native-FP64 path 1e-12."""
+    t = np.arange(ring) * 2 * np.pi / ring
+    pts = np.concatenate([[[0.0, 0.0, -1.0], [0.0, 0.0, 1.0]],
+                          np.stack([np.cos(t), np.sin(t), 0.1 * np.sin(3 * t)], 1)])
+    el = np.array([[0, 2 + k, 2 + (k + 1) % ring, 1] for k in range(ring)], dtype=np.int64)
+    g = np.random.default_rng(ring).normal(size=ring)
+    kappa = np.exp(g)
+    mesh = tg.Mesh(points=torch.tensor(pts, device=DEV), cells={"tetra": torch.tensor(el, device=DEV)})
+    for cls, key, form in ((KappaLaplace, "kappa", "laplace"), (EElasticity, "E", "elasticity")):
+        ip, ix, dv = fem.assemble_csr(pts, el, "tetra", form, 1, coef=kappa)
+        sliver = ring > 40
+        cases = [(torch.float64, "emulated", 1e-10 if sliver else 1e-12),
+                 (torch.float32, "emulated", 1e-3 if sliver else 1e-5)]
+        if sliver:
+            cases.append((torch.float64, "native", 1e-12))
+        for dt, precision, tol in cases:
+            asm = cls.from_mesh(mesh, quadrature_order=1)
+            asm.precision = precision
+            K = asm(mesh.points.to(dt), element_data={key: torch.tensor(kappa, dtype=dt, device=DEV)})
+            assert np.array_equal(K.indptr.cpu().numpy(), ip) and np.array_equal(K.indices.cpu().numpy(), ix)
+            assert rel_err(K.values.cpu().numpy(), dv) <= tol, (form, dt, precision)
