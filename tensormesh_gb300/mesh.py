@@ -1,11 +1,23 @@
 """Mesh container with the reference's accessors, plus structured generators.
 
-Mirrors the parts of TensorMesh's ``Mesh`` (mesh/mesh.py:86-145 constructor,
-403-486 ``elements``, 633-652 ``boundary_mask``) that the assembly path
-reads: ``points [N, D]``, ``cells {type: [E, B]}``, ``point_data``,
+Mirrors TensorMesh's ``Mesh`` (mesh/mesh.py:86-145 constructor, 227-323
+``to_meshio``/``save``, 403-486 ``elements``, 617-652 ``n_elements`` and
+``boundary_mask``, 654-669 ``default_element_type``, 693-740
+``from_meshio``/``read``): ``points [N, D]``, ``cells {type: [E, B]}``,
+``point_data``, ``cell_data {key: {type: [E, ...]}}``, ``field_data``,
 ``default_element_type``, ``elements()``, ``boundary_mask``, ``dtype``,
-``device`` and ``.to``.  A meshio-like object (``.points``, ``.cells`` with
-``.type``/``.data``, ``.point_data``) is accepted directly.
+``device`` and ``.to``.
+
+A meshio mesh (any object with ``.points``, ``.cells`` holding
+``.type``/``.data`` blocks, and optionally ``.point_data``, ``.cell_data``,
+``.field_data``, ``.cell_sets``) is accepted as it comes from a file: every
+cell block is kept (blocks of one type are concatenated in block order, as
+``meshio.Mesh.cells_dict`` does), so a gmsh volume mesh with its line and
+boundary-triangle blocks loads; the default element type is the
+highest-dimensional one and the points keep that many coordinates.  Element
+types the GPU kernels do not cover are stored and raise only when an
+assembler is built on them.  ``reorder=True`` converts P2 connectivity from
+the Gmsh/VTK node order to the internal one (element.py:108-136).
 
 The generators build the structured meshes of the benchmark configurations
 without gmsh: split unit squares (2 triangles per cell) and Kuhn cubes (6
@@ -14,56 +26,139 @@ and P2 versions by edge-midpoint insertion.
 """
 from __future__ import annotations
 
-from typing import Dict, Optional
+import re
+from typing import Dict, Iterable, Optional
 
 import numpy as np
 import torch
 
-from .element import TET_EDGES, TRI_EDGES, element_info
+from .element import TET_EDGES, TRI_EDGES
 
-_DIM_OF = {"triangle": 2, "triangle6": 2, "tetra": 3, "tetra10": 3}
+# Spatial dimension by element-name prefix (element/element_type2dimension.py:
+# every entry there is its prefix's dimension; the trailing digits give the
+# node count).
+_DIM_OF_PREFIX = {"vertex": 0, "line": 1, "polygon": 2, "triangle": 2, "quad": 2,
+                  "tetra": 3, "hexahedron": 3, "wedge": 3, "pyramid": 3}
 # Kuhn tetrahedra: one per permutation of the axes (x=0, y=1, z=2).
 KUHN_PERMUTATIONS = ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0))
+# Midside nodes in the Gmsh/VTK (meshio) order: triangle6 nodes 3-5 sit on
+# edges 01, 12, 20; tetra10 nodes 4-9 on edges 01, 12, 02, 03, 13, 23.
+_VTK_EDGES = {"triangle6": ((0, 1), (1, 2), (0, 2)),
+              "tetra10": ((0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3))}
+
+
+def element_dimension(element_type: str) -> int:
+    m = re.match(r"[a-zA-Z]+", element_type)
+    if m is None or m.group(0) not in _DIM_OF_PREFIX:
+        raise ValueError(f"unknown element type {element_type!r}")
+    return _DIM_OF_PREFIX[m.group(0)]
+
+
+def gmsh_permutation(element_type: str, n_nodes: int) -> torch.Tensor:
+    """perm with ``internal = gmsh[..., perm]`` (the reference's
+    ``get_gmsh_permutation``, element.py:139-152, 1767-1800, 2020-2080).
+
+    Vertices come first in both orders.  The internal P2 order lists the
+    midside node of edge TRI_EDGES[k] / TET_EDGES[k] at position d+1+k; its
+    Gmsh/VTK position is that edge's index in the VTK edge list.  Linear
+    simplices, lines and vertices keep their order."""
+    prefix = re.match(r"[a-zA-Z]+", element_type).group(0)
+    if prefix in ("vertex", "line") or element_type in ("triangle", "tetra"):
+        return torch.arange(n_nodes)
+    if element_type in _VTK_EDGES:
+        vtk, local = _VTK_EDGES[element_type], (TRI_EDGES if prefix == "triangle" else TET_EDGES)
+        nv = 3 if prefix == "triangle" else 4
+        mid = [nv + vtk.index(tuple(sorted(e))) for e in local]
+        return torch.tensor(list(range(nv)) + mid)
+    raise NotImplementedError(f"reordering {element_type} connectivity is not provided")
+
+
+def reorder_connectivity(element_type: str, elements: torch.Tensor, to_gmsh: bool = True) -> torch.Tensor:
+    """Connectivity between the internal and the Gmsh/VTK node order
+    (``Element.reorder``, element.py:108-136)."""
+    perm = gmsh_permutation(element_type, elements.shape[-1]).to(elements.device)
+    if to_gmsh:
+        perm = torch.argsort(perm)
+    return elements.index_select(-1, perm)
+
+
+def _meshio():
+    try:
+        import meshio
+    except ImportError as e:
+        raise ImportError("reading, writing and exporting meshes needs the meshio package") from e
+    return meshio
+
+
+def _flag_to_bool(key, v):
+    if key.startswith("is_") or key.endswith("_mask"):  # mesh.py:104-114
+        return v.bool()
+    return v
 
 
 class Mesh:
-    def __init__(self, mesh=None, *, points=None, cells: Optional[Dict[str, torch.Tensor]] = None,
-                 point_data: Optional[Dict[str, torch.Tensor]] = None):
+    def __init__(self, mesh=None, reorder: bool = False, *, points=None,
+                 cells: Optional[Dict[str, torch.Tensor]] = None,
+                 point_data: Optional[Dict[str, torch.Tensor]] = None,
+                 cell_data: Optional[Dict[str, Dict[str, torch.Tensor]]] = None,
+                 field_data: Optional[Dict[str, torch.Tensor]] = None, cell_sets=None):
         if mesh is not None:
-            pts = np.asarray(mesh.points)
-            cells = {}
-            for c in mesh.cells:
-                cells[c.type] = torch.as_tensor(np.asarray(c.data)).long()
-            point_data = {k: torch.as_tensor(np.asarray(v)) for k, v in getattr(mesh, "point_data", {}).items()}
-            dim = max(_DIM_OF.get(k, 0) for k in cells)
-            points = torch.as_tensor(pts[:, :dim])
+            blocks = {}
+            data_blocks = {}
+            for i, c in enumerate(mesh.cells):
+                blocks.setdefault(c.type, []).append(np.asarray(c.data))
+                for key, per_block in getattr(mesh, "cell_data", {}).items():
+                    data_blocks.setdefault(key, {}).setdefault(c.type, []).append(np.asarray(per_block[i]))
+            cells = {k: torch.from_numpy(np.concatenate(v)).long() for k, v in blocks.items()}
+            if reorder:
+                cells = {k: reorder_connectivity(k, v, to_gmsh=False) for k, v in cells.items()}
+            cell_data = {key: {t: torch.from_numpy(np.concatenate(v)) for t, v in per_type.items()}
+                         for key, per_type in data_blocks.items()}
+            point_data = {k: torch.from_numpy(np.asarray(v)) for k, v in getattr(mesh, "point_data", {}).items()}
+            field_data = {k: torch.from_numpy(np.asarray(v)) for k, v in getattr(mesh, "field_data", {}).items()}
+            cell_sets = dict(getattr(mesh, "cell_sets", {}) or {})
+            dim = max(element_dimension(k) for k in cells)
+            points = torch.from_numpy(np.asarray(mesh.points)[:, :dim])
         if points is None or cells is None:
             raise ValueError("Mesh needs a meshio-like object or points= and cells=")
+        if len(cells) == 0:
+            raise ValueError("Mesh needs at least one cell block")
         self.points = torch.as_tensor(points)
         self.cells = {k: torch.as_tensor(v).long() for k, v in cells.items()}
-        self.point_data = {}
-        for k, v in (point_data or {}).items():
-            v = torch.as_tensor(v)
-            if k.startswith("is_") or k.endswith("_mask"):  # mesh.py:104-107
-                v = v.bool()
-            self.point_data[k] = v
+        self.dim2eletyp: Dict[int, list] = {}
         for k in self.cells:
-            element_info(k)  # raises for element types off the GPU path
+            self.dim2eletyp.setdefault(element_dimension(k), []).append(k)
+        self.point_data = {k: _flag_to_bool(k, torch.as_tensor(v)) for k, v in (point_data or {}).items()}
+        self.cell_data = {k: {t: _flag_to_bool(k, torch.as_tensor(v)) for t, v in d.items()}
+                          for k, d in (cell_data or {}).items()}
+        self.field_data = {k: _flag_to_bool(k, torch.as_tensor(v)) for k, v in (field_data or {}).items()}
+        self.cell_sets = dict(cell_sets or {})
 
     # -- reference accessors ---------------------------------------------------
     @property
-    def default_element_type(self) -> str:
-        dim = max(_DIM_OF[k] for k in self.cells)
-        types = [k for k in self.cells if _DIM_OF[k] == dim]
-        return types[0] if len(types) == 1 else types
+    def default_element_type(self):
+        """The highest-dimensional element type, or the list of them when
+        several share that dimension (mesh.py:133-137)."""
+        types = self.dim2eletyp[max(self.dim2eletyp)]
+        return types[0] if len(types) == 1 else list(types)
 
     def elements(self, element_type=None):
+        """mesh.py:403-486: None -> the default type (a tensor, or a dict for
+        several), "all" -> every block, an int -> the blocks of that dimension
+        (-1: the mesh's), a str -> that block, an iterable -> those blocks."""
         if element_type is None:
             t = self.default_element_type
             return self.cells[t] if isinstance(t, str) else {k: self.cells[k] for k in t}
-        if element_type == "all":
-            return dict(self.cells)
-        return self.cells[element_type]
+        if isinstance(element_type, str):
+            if element_type == "all":
+                return dict(self.cells)
+            return self.cells[element_type]
+        if isinstance(element_type, int):
+            d = self.dim if element_type == -1 else element_type
+            return {k: self.cells[k] for k in self.dim2eletyp.get(d, [])}
+        if isinstance(element_type, Iterable):
+            return {k: self.cells[k] for k in element_type}
+        raise TypeError(f"element_type must be str, int or Iterable[str], got {element_type!r}")
 
     @property
     def boundary_mask(self) -> torch.Tensor:
@@ -83,7 +178,9 @@ class Mesh:
 
     @property
     def n_elements(self) -> int:
-        return sum(int(v.shape[0]) for v in self.cells.values())
+        """Elements of the default type(s) (mesh.py:617-631)."""
+        t = self.default_element_type
+        return sum(int(self.cells[k].shape[0]) for k in ([t] if isinstance(t, str) else t))
 
     @property
     def dtype(self) -> torch.dtype:
@@ -97,15 +194,65 @@ class Mesh:
         pts = self.points.to(device=device) if device is not None else self.points
         if dtype is not None:
             pts = pts.to(dtype)
-        m = Mesh(points=pts, cells={k: v.to(pts.device) for k, v in self.cells.items()},
-                 point_data={k: v.to(pts.device) for k, v in self.point_data.items()})
-        return m
+        d = pts.device
+        return Mesh(points=pts, cells={k: v.to(d) for k, v in self.cells.items()},
+                    point_data={k: v.to(d) for k, v in self.point_data.items()},
+                    cell_data={k: {t: v.to(d) for t, v in per.items()} for k, per in self.cell_data.items()},
+                    field_data={k: v.to(d) for k, v in self.field_data.items()}, cell_sets=self.cell_sets)
 
     def double(self) -> "Mesh":
         return self.to(dtype=torch.float64)
 
     def float(self) -> "Mesh":
         return self.to(dtype=torch.float32)
+
+    # -- meshio round trip -------------------------------------------------------
+    @classmethod
+    def from_meshio(cls, mesh, reorder: bool = False) -> "Mesh":
+        return cls(mesh, reorder)
+
+    @classmethod
+    def read(cls, file_name: str, file_format: Optional[str] = None, reorder: bool = False) -> "Mesh":
+        return cls(_meshio().read(file_name, file_format), reorder)
+
+    from_file = read
+
+    def to_meshio(self, reorder: bool = False):
+        """An in-memory ``meshio.Mesh`` (mesh.py:227-260); ``reorder=True``
+        writes connectivity in the Gmsh/VTK order."""
+        meshio = _meshio()
+        cells = {}
+        for k, v in self.cells.items():
+            conn = v.detach().cpu()
+            cells[k] = (reorder_connectivity(k, conn, to_gmsh=True) if reorder else conn).numpy()
+        order = list(cells)
+        return meshio.Mesh(
+            points=self.points.detach().cpu().numpy(), cells=cells,
+            point_data={k: v.detach().cpu().numpy() for k, v in self.point_data.items()},
+            cell_data={k: [per[t].detach().cpu().numpy() for t in order if t in per]
+                       for k, per in self.cell_data.items()},
+            field_data={k: v.detach().cpu().numpy() for k, v in self.field_data.items()},
+            cell_sets=self.cell_sets)
+
+    def save(self, file_name: str, file_format: Optional[str] = None) -> "Mesh":
+        """``meshio.write`` (mesh.py:267-323): flag arrays become floats; a
+        .vtk/.vtu file gets Gmsh/VTK connectivity, 3-D points, a zero ``u``
+        point field when there is none, and no cell sets."""
+        vtk = file_name.endswith((".vtk", ".vtu"))
+        m = self.to_meshio(reorder=vtk)
+        flag = lambda k: k.startswith("is_") or k.endswith("_mask")
+        m.point_data = {k: (v.astype(float) if flag(k) else v) for k, v in m.point_data.items()}
+        m.cell_data = {k: [(b.astype(float) if flag(k) else b) for b in v] for k, v in m.cell_data.items()}
+        m.field_data = {k: (v.astype(float) if flag(k) else v) for k, v in m.field_data.items()}
+        if vtk:
+            if m.points.shape[1] == 2:
+                m.points = np.concatenate([m.points, np.zeros((m.points.shape[0], 1))], -1)
+            m.point_data.setdefault("u", np.zeros((m.points.shape[0],)))
+            m.cell_sets = {}
+        _meshio().write(file_name, m, file_format)
+        return self
+
+    to_file = save
 
     # -- structured generators ---------------------------------------------------
     @staticmethod
