@@ -358,6 +358,125 @@ def assemble_load(points, elements, element_type, quadrature_order, kind, value=
 
 
 # ---------------------------------------------------------------------------
+# Facet (boundary) loads: assemble/facet_assembler.py.
+# ---------------------------------------------------------------------------
+# Facet f of a simplex is the facet opposite vertex f; its nodes are the other
+# vertices and, for P2, the midpoints of the edges between them
+# (element.py:1411-1440 element_to_facet; Triangle.edge, Tetrahedron.face).
+_FACET_VERTICES = {2: [(1, 2), (0, 2), (0, 1)], 3: [(1, 2, 3), (0, 2, 3), (0, 1, 3), (0, 1, 2)]}
+
+
+def facet_nodes(element_type: str) -> np.ndarray:
+    """Local node ids of each facet [F, nodes per facet]."""
+    dim, nb, p = ELEMENTS[element_type]
+    out = []
+    for vs in _FACET_VERTICES[dim]:
+        nodes = list(vs)
+        if p == 2:
+            edges = _TRI_EDGES if dim == 2 else _TET_EDGES
+            nodes += [dim + 1 + k for k, (i, j) in enumerate(edges) if i in vs and j in vs]
+        out.append(nodes)
+    return np.array(out, dtype=np.int64)
+
+
+def facet_rule(dim: int, order: int):
+    """Facet-local rule (weights [Qf], points [Qf, D-1]): Gauss-Legendre with
+    ``order`` points moved to [0, 1] for edges (element/quadrature.py:9-66
+    lin_quadrature), the triangle rule for faces (tri_quadrature)."""
+    if dim == 2:
+        x, w = np.polynomial.legendre.leggauss(order)
+        return 0.5 * w, (0.5 * (x + 1.0))[:, None]
+    return np.array(_TRI_W[order], dtype=np.float64), np.array(_TRI_P[order], dtype=np.float64)
+
+
+def facet_quadrature(element_type: str, order: int):
+    """Exact float64 facet quadrature in cell reference coordinates.
+
+    Returns (w [F, Qf], xi [F, Qf, D], tangents [F, D-1, D]): facet f is the
+    affine image r -> P_a + sum_k r_k (P_{v_k+1} - P_a) of the reference
+    segment / triangle, P the reference simplex's vertices and (a, v_1, ...)
+    the facet's vertices in order (element.py:993-1066
+    get_local_facet_mapping_fns; quadrature.py:321-410 pushes the rule through
+    it).  The reference evaluates this table in float32
+    (transformation.py:519-531 leaves get_facet_quadrature's float32 default),
+    so its float64 facet integrals carry float32 rounding of w and xi; pass its
+    table as ``tables`` to facet_load to reproduce it."""
+    dim = ELEMENTS[element_type][0]
+    P = np.concatenate([np.zeros((1, dim)), np.eye(dim)], 0)
+    w, r = facet_rule(dim, order)
+    xi, tang = [], []
+    for vs in _FACET_VERTICES[dim]:
+        T = np.stack([P[v] - P[vs[0]] for v in vs[1:]], 0)       # [D-1, D]
+        xi.append(P[vs[0]][None, :] + r @ T)
+        tang.append(T)
+    F = len(xi)
+    return np.broadcast_to(w, (F, w.shape[0])).copy(), np.stack(xi), np.stack(tang)
+
+
+def facet_select(elements: np.ndarray, element_type: str, boundary_mask: np.ndarray):
+    """(element ids, local facet ids) of the facets whose nodes are all
+    flagged, element-major (facet_assembler.py:491-508: facet candidates of
+    the elements touching the mask, kept when ``mask[facet].all(-1)``,
+    ``nonzero`` order)."""
+    fn = facet_nodes(element_type)
+    sel = np.asarray(boundary_mask, dtype=bool)[elements[:, fn]].all(-1)   # [E, F]
+    e, f = np.nonzero(sel)
+    return e, f
+
+
+def facet_load(points, elements, element_type, boundary_mask, quadrature_order, kind, value=None,
+               tables=None):
+    """Facet load b_i = sum over selected facets, facet quadrature points of
+    g(x_q) N_i(xi_q) w_q |F_q| (facet_assembler.py:195-235 same-facet branch:
+    integrand, einsum with FxW, ReduceProjector over the whole cell's nodes).
+
+    |F| = sqrt(det(F F^T)) with F = d(gamma)/dr . J, J[i, j] = sum_b
+    dN_b/dxi_i X_b[j] evaluated at the float64 facet points
+    (transformation.py:993-1003 detF, element.py:1295-1409
+    eval_facet_jacobian, 1203-1293 eval_facet_cell_jacobian); the shape values
+    and weights come from ``tables`` = (w [F, Qf], xi [F, Qf, D]) when given,
+    else from the exact rule (facet_quadrature).
+
+    kind as for assemble_load: "const" (scalar or [H]), "point" (node data
+    [N] or [N, H] interpolated with the facet shape values), "func" (callable
+    of x [..., D], x interpolated with the facet shape values).
+    """
+    dim = ELEMENTS[element_type][0]
+    w_ex, xi_ex, tang = facet_quadrature(element_type, quadrature_order)
+    w_t, xi_t = (w_ex, xi_ex) if tables is None else (np.asarray(tables[0], np.float64),
+                                                       np.asarray(tables[1], np.float64))
+    F, Qf = xi_t.shape[:2]
+    N_t = np.stack([shape_functions(element_type, xi_t[f])[0] for f in range(F)])      # [F, Qf, B]
+    dN_ex = np.stack([shape_functions(element_type, xi_ex[f])[1] for f in range(F)])   # [F, Qf, D, B]
+    e, f = facet_select(elements, element_type, boundary_mask)
+    X = points[elements[e]]                                                            # [S, B, D]
+    J = np.einsum("sbj,sqib->sqij", X, dN_ex[f])
+    T = np.einsum("ski,sqij->sqkj", tang[f], J)                                        # [S, Qf, D-1, D]
+    detF = np.sqrt(np.linalg.det(T @ np.swapaxes(T, -1, -2)))
+    fxw = w_t[f] * detF                                                                # [S, Qf]
+    Ns = N_t[f]                                                                        # [S, Qf, B]
+    if kind == "const":
+        c = np.atleast_1d(np.asarray(value, dtype=np.float64))
+        fq = np.broadcast_to(c, (len(e), Qf, c.shape[0]))
+    elif kind == "point":
+        pv = np.asarray(value, dtype=np.float64)
+        if pv.ndim == 1:
+            pv = pv[:, None]
+        fq = np.einsum("sbh,sqb->sqh", pv[elements[e]], Ns)
+    elif kind == "func":
+        xq = np.einsum("sbd,sqb->sqd", X, Ns)
+        fv = np.asarray(value(xq), dtype=np.float64)
+        fq = fv[..., None] if fv.ndim == 2 else fv
+    else:
+        raise ValueError(kind)
+    be = np.einsum("sqh,sqb,sq->sbh", fq, Ns, fxw)
+    H = be.shape[-1]
+    out = np.zeros((points.shape[0], H))
+    np.add.at(out, elements[e].reshape(-1), be.reshape(-1, H))
+    return out.reshape(-1) if H > 1 else out[:, 0]
+
+
+# ---------------------------------------------------------------------------
 # Condenser (operator/condense.py:182-220 layout, 238-309 call, 429-458
 # recover).  Boolean-mask compaction keeps CSR order.
 # ---------------------------------------------------------------------------

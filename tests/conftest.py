@@ -9,6 +9,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "reference_fem.npz")
+GOLDEN_FACET = os.path.join(ROOT, "tests", "golden", "reference_facet.npz")
 
 
 def pytest_configure(config):
@@ -32,3 +33,8 @@ def pytest_collection_modifyitems(config, items):
 @pytest.fixture(scope="session")
 def golden():
     return dict(np.load(GOLDEN))
+
+
+@pytest.fixture(scope="session")
+def golden_facet():
+    return dict(np.load(GOLDEN_FACET))

@@ -10,7 +10,7 @@ The reference needs two packages that are not installed here (``meshio`` and
 reference touches on this path (no numerics).  The fixtures written are small
 ``.npz`` files: every array in them is an input this script built or an
 output of the reference's own ``ElementAssembler`` / ``NodeAssembler`` /
-``Condenser`` / ``SparseSolveScipy`` calls.  Tests read only the ``.npz``
+``FacetAssembler`` / ``Condenser`` / ``SparseSolveScipy`` calls.  Tests read only the ``.npz``
 files, never the reference.
 """
 from __future__ import annotations
@@ -261,6 +261,73 @@ def main(ref_root):
             out[f"{etype}/nh/q{q}/grad_u"] = u.grad.numpy().copy()
     np.savez_compressed(os.path.join(HERE, "reference_fem.npz"), **out)
     print("wrote", len(out), "arrays")
+    facet_fixtures(tm, torch, meshes, mk_mesh)
+
+
+def facet_fixtures(tm, torch, meshes, mk_mesh):
+    """Boundary loads of the reference FacetAssembler on the form meshes, on
+    P2 meshes with curved facets (every midpoint moved), with the default
+    boundary mask and with a one-side mask; plus the reference's float32
+    facet quadrature tables (points in cell coordinates, weights)."""
+    from tensormesh.element.element import Tetrahedron, Triangle
+
+    class FacetOne(tm.FacetAssembler):
+        def forward(self, v):
+            return v
+
+    class FacetVector(tm.FacetAssembler):
+        def forward(self, v):
+            t = torch.tensor([0.5, -1.0] if v.shape[0] in (3, 6) else [0.0, 0.3, -1.0], dtype=v.dtype)
+            return v[:, None] * t
+
+    class FacetFunc(tm.FacetAssembler):
+        def forward(self, x, v):
+            return (torch.sin(math.pi * x[0]) + x[1] ** 2) * v
+
+    class FacetPoint(tm.FacetAssembler):
+        def forward(self, v, g):
+            return g * v
+
+    out = {}
+    rng = np.random.default_rng(17)
+    # "top": the nodes on the side x_{D-1} = 1 (flagged before the midpoints move)
+    facet_meshes = {k: (p, c, b, np.isclose(p[:, -1], 1.0)) for k, (p, c, b) in meshes.items()}
+    for name, base, amp in (("triangle6c", "triangle", 0.02), ("tetra10c", "tetra", 0.04)):
+        pts, cells, bd = to_p2(*meshes[base])
+        top = np.isclose(pts[:, -1], 1.0)
+        pts = pts.copy()
+        nv = meshes[base][0].shape[0]
+        pts[nv:] += rng.uniform(-amp, amp, pts[nv:].shape)
+        facet_meshes[name] = (pts, cells, bd, top)
+    for etype, (pts, cells, bd, top) in facet_meshes.items():
+        ref_type = etype.rstrip("c")
+        mesh = mk_mesh(pts, cells, bd, ref_type)
+        dim = pts.shape[1]
+        mesh.register_point_data("is_top", torch.from_numpy(top))
+        g = np.cos(2.0 * pts[:, 0]) + 0.5 * pts[:, dim - 1]
+        out[f"{etype}/points"] = pts
+        out[f"{etype}/elements"] = cells
+        out[f"{etype}/boundary"] = bd
+        out[f"{etype}/top"] = top
+        out[f"{etype}/facet_g"] = g
+        for q in (1, 2, 3, 4):
+            cases = {
+                "const": lambda: FacetOne.from_mesh(mesh, quadrature_order=q)(mesh.points),
+                "vector": lambda: FacetVector.from_mesh(mesh, quadrature_order=q)(mesh.points),
+                "func": lambda: FacetFunc.from_mesh(mesh, quadrature_order=q)(mesh.points),
+                "point": lambda: FacetPoint.from_mesh(mesh, quadrature_order=q)(
+                    mesh.points, point_data={"g": torch.from_numpy(g)}),
+                "top": lambda: FacetOne.from_mesh(mesh, boundary_mask="is_top", quadrature_order=q)(mesh.points),
+            }
+            for case, fn in cases.items():
+                out[f"{etype}/facet_{case}/q{q}"] = fn().detach().numpy().astype(np.float64)
+    for cls, key in ((Triangle, "triangle"), (Tetrahedron, "tetra")):
+        for q in (1, 2, 3, 4):
+            w, p = cls.get_facet_quadrature(q, transform=True)
+            out[f"facet_table/{key}/q{q}/w"] = w.numpy().astype(np.float64)
+            out[f"facet_table/{key}/q{q}/p"] = p.numpy().astype(np.float64)
+    np.savez_compressed(os.path.join(HERE, "reference_facet.npz"), **out)
+    print("wrote", len(out), "facet arrays")
 
 
 if __name__ == "__main__":

@@ -112,3 +112,51 @@ def test_oracle_neo_hookean_zero_displacement_has_zero_energy(golden):
     pts, el = golden["triangle/points"], golden["triangle/elements"]
     e, g = fem.neo_hookean(pts, el, "triangle", 2, np.zeros_like(pts), 1.0, 0.3)
     assert abs(e) <= 1e-14 and np.max(np.abs(g)) <= 1e-14
+
+
+FACET_MESHES = ["triangle", "triangle6", "tetra", "tetra10", "triangle6c", "tetra10c"]
+
+
+def facet_cases(g, et):
+    """(kind, value, mask) per fixture case (the forwards of make_golden.py's
+    facet_fixtures)."""
+    pts = g[f"{et}/points"]
+    dim = pts.shape[1]
+    bd, top = g[f"{et}/boundary"], g[f"{et}/top"]
+    return {
+        "const": ("const", 1.0, bd),
+        "vector": ("const", [0.5, -1.0] if dim == 2 else [0.0, 0.3, -1.0], bd),
+        "func": ("func", lambda x: np.sin(math.pi * x[..., 0]) + x[..., 1] ** 2, bd),
+        "point": ("point", g[f"{et}/facet_g"], bd),
+        "top": ("const", 1.0, top),
+    }
+
+
+@pytest.mark.parametrize("et", FACET_MESHES)
+@pytest.mark.parametrize("q", [1, 2, 3, 4])
+def test_oracle_facet_loads_match_reference(golden_facet, et, q):
+    """With the reference's own float32 facet table the restatement reproduces
+    the reference to rounding; with the exact float64 table (what the GPU path
+    uses) the difference is the reference table's float32 rounding."""
+    g = golden_facet
+    etype = et.rstrip("c")
+    fam = "triangle" if etype.startswith("tri") else "tetra"
+    table = (g[f"facet_table/{fam}/q{q}/w"], g[f"facet_table/{fam}/q{q}/p"])
+    pts, el = g[f"{et}/points"], g[f"{et}/elements"]
+    for case, (kind, val, mask) in facet_cases(g, et).items():
+        ref = g[f"{et}/facet_{case}/q{q}"]
+        got = fem.facet_load(pts, el, etype, mask, q, kind, val, tables=table)
+        assert rel_err(got, ref) <= 1e-12, (case, rel_err(got, ref))
+        exact = fem.facet_load(pts, el, etype, mask, q, kind, val)
+        assert rel_err(exact, ref) <= 1e-6, (case, rel_err(exact, ref))
+
+
+def test_oracle_facet_selection_includes_interior_facets(golden_facet):
+    """The reference selects every facet whose nodes are all flagged: on the
+    4 x 4 square the corner-cell diagonals joining two boundary nodes are
+    integrated from both sides (boundary length 4 + 2 * 2 * sqrt(2) / 4)."""
+    g = golden_facet
+    tot = fem.facet_load(g["triangle/points"], g["triangle/elements"], "triangle", g["triangle/boundary"], 2,
+                         "const", 1.0).sum()
+    assert abs(tot - (4 + math.sqrt(2))) < 1e-12
+    assert abs(g["triangle/facet_const/q2"].sum() - tot) < 1e-12
