@@ -270,6 +270,24 @@ def run_ours(args):
         if os.path.exists(peaks_path_):
             fp32["hbm_frac"] = fp32["achieved_gbs"] / float(json.load(open(peaks_path_))["hbm_gbs"])
 
+    # ---- boundary traction load (FacetAssembler) on the same 128^3 mesh, FP64
+    facet = None
+    if not args.no_extra:
+        class Traction(tg.FacetAssembler):
+            def forward(self, v):
+                return v[:, None] * torch.tensor([0.0, 0.3, -1.0], dtype=v.dtype, device=v.device)
+        t0 = time.perf_counter()
+        fasm = Traction.from_mesh(mesh, quadrature_order=2)
+        torch.cuda.synchronize()
+        f_setup = time.perf_counter() - t0
+        ms_f = time_calls(lambda: fasm(mesh.points))
+        S = fasm.topology.n_sel
+        facet = {"workload": "128^3 Kuhn cube, traction (0, 0.3, -1) on every facet with all nodes on the boundary, "
+                             "facet rule of order 2, FP64",
+                 "facets": S, "ms_per_load": ms_f, "facets_per_s": S / (ms_f * 1e-3),
+                 "setup_seconds": round(f_setup, 3)}
+        del fasm
+
     # ---- 64^3 P1-tet linear elasticity, per-element E, FP64 (secondary)
     elast = None
     hyper = None
@@ -512,6 +530,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "fp32_variant": fp32,
             "elasticity_64cube": elast,
+            "facet_traction_128cube": facet,
             "neo_hookean_energy": hyper,
             "adjoint_256_square": adjoint,
             "batched_256_meshes": batched,

@@ -274,6 +274,26 @@ int tm_neohookean(int32_t element, int32_t dtype, int32_t n_quad, const double* 
                   const int32_t* elements, int64_t n_elements, const void* u, double mu, double lam,
                   double* energy_el, void* grad_el, void* stream);
 
+/*
+ * Facet (boundary) load contributions (replaces FacetAssembler.__call__,
+ * assemble/facet_assembler.py:130-235, for integrands g * v).  Per selected
+ * facet s (sel[s] = element * F + local facet f; F = 3 for triangles, 4 for
+ * tetrahedra; facet f is the one opposite vertex f) and cell node b:
+ *   out[s][b][h] = sum_q w[f][q] |F_q| g_h(q) N[f][q][b],
+ * |F_q| = |t_0| (edges) or |t_0 x t_1| (faces), t_k = sum_b Tc[f][q][k][b] X_b.
+ * tables (float64): w [F][Qf], N [F][Qf][B], Tc [F][Qf][D-1][B].
+ * coef_kind: TM_COEF_SCALAR (scal: HOST array of n_comp values),
+ * TM_COEF_POINT (coef [N][n_comp] in dtype, interpolated with N),
+ * TM_COEF_QUAD (coef [n_sel][Qf][n_comp] in dtype).  n_comp <= 3.
+ * With x_out non-NULL the call writes only the physical facet quadrature
+ * points x_out [n_sel][Qf][D] (dtype), for callers that evaluate g(x).
+ * out [n_sel][B][n_comp] in dtype; FP64 arithmetic.  The caller reduces out
+ * to the nodes (tm_segment_sum in a fixed order).
+ */
+int tm_facet_load(int32_t element, int32_t dtype, int32_t n_quad, const double* tables, const void* points,
+                  const int32_t* elements, const int64_t* sel, int64_t n_sel, int32_t coef_kind, const void* coef,
+                  const double* scal, int32_t n_comp, void* out, void* x_out, void* stream);
+
 /* y = A x for CSR A (replaces SparseMatrix @ / spmv, sparse/mm/__init__.py:
  * 22-72).  dtype applies to values, x and y; nnz = indptr[n_rows] (it sets
  * the lanes per row; the row extents come from indptr). */

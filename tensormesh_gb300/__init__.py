@@ -5,7 +5,7 @@ SpMV / Jacobi-PCG -- behind the reference's own Python API.
 Exports mirror ``tensormesh/__init__.py``: Mesh, Condenser, ElementAssembler,
 NodeAssembler, LaplaceElementAssembler, MassElementAssembler,
 LinearElasticityElementAssembler, const_node_assembler, func_node_assembler,
-plus SparseMatrix.
+FacetAssembler, plus SparseMatrix.
 """
 from .mesh import Mesh
 from .sparse import SparseMatrix
@@ -13,7 +13,8 @@ from .assemble import (ElementAssembler, NodeAssembler, LaplaceElementAssembler,
                        LinearElasticityElementAssembler, const_node_assembler, func_node_assembler)
 from .condense import Condenser
 from .energy import NeoHookeanModel
+from .facet import FacetAssembler
 
 __all__ = ["Mesh", "SparseMatrix", "ElementAssembler", "NodeAssembler", "LaplaceElementAssembler",
            "MassElementAssembler", "LinearElasticityElementAssembler", "const_node_assembler",
-           "func_node_assembler", "Condenser", "NeoHookeanModel"]
+           "func_node_assembler", "Condenser", "NeoHookeanModel", "FacetAssembler"]

@@ -36,7 +36,7 @@ EXPORTS = [
     "tm_batched_assemble_pcg", "tm_batched_max_clusters", "tm_patch_smem_bytes",
     "tm_mpnn_input_fwd", "tm_mpnn_layer_fwd", "tm_mpnn_readout_fwd", "tm_mpnn_readout_bwd",
     "tm_mpnn_layer_bwd", "tm_mpnn_input_bwd", "tm_gather_axpy_f32",
-    "tm_pcg_jacobi_noalloc", "tm_twolevel_apply", "tm_neohookean",
+    "tm_pcg_jacobi_noalloc", "tm_twolevel_apply", "tm_neohookean", "tm_facet_load",
 ]
 
 P = ctypes.c_void_p
@@ -134,6 +134,7 @@ def _declare(lib):
                                   ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_double), P],
         "tm_twolevel_apply": [ctypes.POINTER(TwoLevel), P, P, P],
         "tm_neohookean": [i32, i32, i32, P, P, P, i64, P, ctypes.c_double, ctypes.c_double, P, P, P],
+        "tm_facet_load": [i32, i32, i32, P, P, P, P, i64, i32, P, ctypes.POINTER(ctypes.c_double), i32, P, P, P],
     }
     lib.tm_patch_smem_bytes.argtypes = [i32, i32, i32, i32, ctypes.POINTER(PatchPlan), i32, i32]
     lib.tm_patch_smem_bytes.restype = i64

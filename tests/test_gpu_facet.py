@@ -1,0 +1,175 @@
+"""Parity of the CUDA facet (boundary) loads against the oracle and the
+reference's own FacetAssembler outputs (golden fixtures).
+
+Bars: float64 within 1e-12 relative (max-norm, relative to max|b|) of the
+oracle with the exact facet rule; within 1e-6 of the reference, whose facet
+rule is rounded to float32 (the oracle reproduces the reference to 1e-12
+when handed the reference's table, tests/test_oracle_golden.py); float32
+within 1e-5; bitwise determinism run to run."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import tensormesh_gb300 as tg
+from oracle import fem
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+MESHES = ["triangle", "triangle6", "tetra", "tetra10", "triangle6c", "tetra10c"]
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+class FacetOne(tg.FacetAssembler):
+    def forward(self, v):
+        return v
+
+
+class FacetVector(tg.FacetAssembler):
+    def forward(self, v):
+        t = torch.tensor([0.5, -1.0] if v.shape[0] in (3, 6) else [0.0, 0.3, -1.0], dtype=v.dtype, device=v.device)
+        return v[:, None] * t
+
+
+class FacetFunc(tg.FacetAssembler):
+    def forward(self, x, v):
+        return (torch.sin(math.pi * x[0]) + x[1] ** 2) * v
+
+
+class FacetPoint(tg.FacetAssembler):
+    def forward(self, v, g):
+        return g * v
+
+
+def mesh_of(g, et, dtype=torch.float64):
+    pts = torch.tensor(g[f"{et}/points"], dtype=dtype, device=DEV)
+    el = torch.tensor(g[f"{et}/elements"], device=DEV)
+    return tg.Mesh(points=pts, cells={et.rstrip("c"): el},
+                   point_data={"is_boundary": torch.tensor(g[f"{et}/boundary"], device=DEV),
+                               "is_top": torch.tensor(g[f"{et}/top"], device=DEV)})
+
+
+def run_case(mesh, case, q, gfield):
+    if case == "const":
+        return FacetOne.from_mesh(mesh, quadrature_order=q)(mesh.points)
+    if case == "vector":
+        return FacetVector.from_mesh(mesh, quadrature_order=q)(mesh.points)
+    if case == "func":
+        return FacetFunc.from_mesh(mesh, quadrature_order=q)(mesh.points)
+    if case == "point":
+        return FacetPoint.from_mesh(mesh, quadrature_order=q)(mesh.points, point_data={"g": gfield})
+    return FacetOne.from_mesh(mesh, boundary_mask="is_top", quadrature_order=q)(mesh.points)
+
+
+def oracle_case(g, et, case, q):
+    pts, el = g[f"{et}/points"], g[f"{et}/elements"]
+    dim = pts.shape[1]
+    bd, top = g[f"{et}/boundary"], g[f"{et}/top"]
+    kind, val, mask = {
+        "const": ("const", 1.0, bd),
+        "vector": ("const", [0.5, -1.0] if dim == 2 else [0.0, 0.3, -1.0], bd),
+        "func": ("func", lambda x: np.sin(math.pi * x[..., 0]) + x[..., 1] ** 2, bd),
+        "point": ("point", g[f"{et}/facet_g"], bd),
+        "top": ("const", 1.0, top),
+    }[case]
+    return fem.facet_load(pts, el, et.rstrip("c"), mask, q, kind, val)
+
+
+@pytest.mark.parametrize("et", MESHES)
+@pytest.mark.parametrize("q", [1, 2, 3, 4])
+@pytest.mark.parametrize("case", ["const", "vector", "func", "point", "top"])
+def test_facet_loads_match_oracle_and_reference(golden_facet, et, q, case):
+    g = golden_facet
+    mesh = mesh_of(g, et)
+    gfield = torch.tensor(g[f"{et}/facet_g"], device=DEV)
+    got = run_case(mesh, case, q, gfield).cpu().numpy()
+    ref = g[f"{et}/facet_{case}/q{q}"]
+    assert got.shape == ref.shape
+    assert rel_err(got, oracle_case(g, et, case, q)) <= 1e-12
+    assert rel_err(got, ref) <= 1e-6
+
+
+@pytest.mark.parametrize("et", MESHES)
+@pytest.mark.parametrize("case", ["const", "vector", "func", "point"])
+def test_facet_loads_fp32(golden_facet, et, case):
+    g = golden_facet
+    mesh = mesh_of(g, et, torch.float32)
+    gfield = torch.tensor(g[f"{et}/facet_g"], device=DEV, dtype=torch.float32)
+    got = run_case(mesh, case, 2, gfield)
+    assert got.dtype == torch.float32
+    assert rel_err(got.cpu().numpy(), oracle_case(g, et, case, 2)) <= 1e-5
+
+
+@pytest.mark.parametrize("etype", ["triangle6", "tetra10"])
+def test_facet_loads_larger_curved_mesh(etype):
+    """More facets (several thread blocks) with curved P2 facets: every
+    midpoint moved, against the oracle."""
+    base = tg.Mesh.gen_unit_square(40) if etype == "triangle6" else tg.Mesh.gen_unit_cube(9)
+    m = base.to_p2()
+    nv = base.n_points
+    gen = torch.Generator().manual_seed(3)
+    pts = m.points.clone()
+    pts[nv:] += 0.1 / 40 * (torch.rand(pts[nv:].shape, generator=gen, dtype=torch.float64) - 0.5)
+    el = m.cells[etype]
+    bd = m.boundary_mask
+    gf = torch.cos(pts[:, 0]) * (1 + pts[:, -1])
+    mesh = tg.Mesh(points=pts.to(DEV), cells={etype: el.to(DEV)}, point_data={"is_boundary": bd.to(DEV)})
+    for q in (2, 3):
+        got = FacetPoint.from_mesh(mesh, quadrature_order=q)(mesh.points, point_data={"g": gf.to(DEV)})
+        ref = fem.facet_load(pts.numpy(), el.numpy(), etype, bd.numpy(), q, "point", gf.numpy())
+        assert rel_err(got.cpu().numpy(), ref) <= 1e-12
+
+
+def test_facet_selection_and_total_measure():
+    """The sum of the constant load is the measure of the selected facets:
+    the unit cube's surface plus the interior faces whose nodes are all on
+    the boundary, each counted from both sides."""
+    mesh = tg.Mesh.gen_unit_cube(6, device=DEV)
+    b = FacetOne.from_mesh(mesh, quadrature_order=1)(mesh.points)
+    el = mesh.cells["tetra"].cpu().numpy()
+    pts = mesh.points.cpu().numpy()
+    bd = mesh.boundary_mask.cpu().numpy()
+    e, f = fem.facet_select(el, "tetra", bd)
+    fn = fem.facet_nodes("tetra")
+    tri = pts[el[e][np.arange(len(e))[:, None], fn[f]]]
+    area = 0.5 * np.linalg.norm(np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0]), axis=1).sum()
+    assert abs(float(b.sum()) - area) <= 1e-12 * area
+    assert area >= 6.0 - 1e-12
+
+
+def test_facet_loads_are_bitwise_deterministic():
+    mesh = tg.Mesh.gen_unit_cube(10, device=DEV)
+    asm = FacetFunc.from_mesh(mesh, quadrature_order=3)
+    ref = asm(mesh.points).clone()
+    for _ in range(4):
+        assert torch.equal(asm(mesh.points), ref)
+
+
+def test_facet_edge_cases():
+    mesh = tg.Mesh.gen_unit_square(4, device=DEV)
+    none = torch.zeros(mesh.n_points, dtype=torch.bool, device=DEV)
+    z = FacetVector.from_mesh(mesh, boundary_mask=none)(mesh.points)
+    assert z.shape == (2 * mesh.n_points,) and not bool(z.any())
+    shared = FacetPoint.from_assembler(FacetOne.from_mesh(mesh))
+    gf = torch.rand(mesh.n_points, dtype=torch.float64, device=DEV)
+    assert torch.equal(shared(mesh.points, point_data={"g": gf}),
+                       FacetPoint.from_mesh(mesh)(mesh.points, point_data={"g": gf}))
+
+    class Square(tg.FacetAssembler):
+        def forward(self, v):
+            return v * v
+
+    with pytest.raises(NotImplementedError):
+        Square.from_mesh(mesh)(mesh.points)
+    with pytest.raises(NotImplementedError):
+        FacetOne.from_mesh(mesh, quadrature_order=5)
+    with pytest.raises(NotImplementedError):
+        FacetOne.from_mesh(mesh)(mesh.points.clone().requires_grad_(True))
+    with pytest.raises(RuntimeError):
+        FacetOne.from_mesh(mesh.to("cpu"))(mesh.points.cpu())
