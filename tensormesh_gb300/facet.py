@@ -26,7 +26,9 @@ reproducible.  The reference builds its facet rule in float32
 (element/transformation.py:519-531 keeps get_facet_quadrature's float32
 default), so its float64 facet loads carry float32 rounding of the points
 and weights (about 3e-7 relative); the rule here is exact in float64.
-Gradients through facet loads are not provided.
+Gradients flow to the ``point_data`` field of a point-data integrand (the load is
+linear in it with a symmetric facet mass matrix); gradients with respect to
+the points are not provided.
 """
 from __future__ import annotations
 
@@ -306,10 +308,41 @@ class FacetAssembler(nn.Module):
         for k, v in point_data.items():
             assert v.shape[0] == self.n_points, f"the shape of {k} should be [n_point, ...], but got {v.shape}"
         _require_cuda(pts, "points")
-        if pts.requires_grad or any(v.requires_grad for v in point_data.values()):
-            raise NotImplementedError("gradients through facet loads are not provided")
+        if pts.requires_grad:
+            raise NotImplementedError("gradients of facet loads with respect to the points are not provided")
         form = self._resolve_form(self.forward if func is None else func, point_data)
+        if form.kind == "point" and point_data[form.coef_key].requires_grad:
+            return _FacetPointLoad.apply(point_data[form.coef_key], self, form, pts)
+        if any(v.requires_grad for v in point_data.values()):
+            raise NotImplementedError("gradients through facet loads are provided for the point_data field "
+                                      "of a point-data integrand only")
         return facet_load(self, form, pts, point_data)
+
+
+class _FacetPointLoad(torch.autograd.Function):
+    """b = (M g) scaled per component, M_ij = sum over selected facets and
+    facet points of w |F| N_i N_j (symmetric), so dL/dg = M (dL/db scaled
+    back): the same kernel run on the incoming gradient."""
+
+    @staticmethod
+    def forward(ctx, g, asm, form, pts):
+        ctx.asm, ctx.form, ctx.pts = asm, form, pts
+        ctx.g_shape = g.shape
+        return facet_load(asm, form, pts, {form.coef_key: g.detach()})
+
+    @staticmethod
+    def backward(ctx, gb):
+        form, N = ctx.form, ctx.asm.n_points
+        H = form.n_comp
+        gb = gb.reshape(N, H)
+        a = form.scale.to(device=gb.device, dtype=gb.dtype)
+        if len(ctx.g_shape) == 1:
+            # scalar field times the factor vector a: dL/dg = M (gb . a)
+            back = FacetForm("point", n_comp=1, coef_key=form.coef_key, scale=torch.ones(1, dtype=torch.float64))
+            grad = facet_load(ctx.asm, back, ctx.pts, {form.coef_key: (gb @ a).contiguous()})
+        else:
+            grad = facet_load(ctx.asm, form, ctx.pts, {form.coef_key: gb.contiguous()})
+        return grad.reshape(ctx.g_shape), None, None, None
 
 
 def facet_load(asm: FacetAssembler, form: FacetForm, pts: torch.Tensor, point_data) -> torch.Tensor:

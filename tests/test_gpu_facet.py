@@ -173,3 +173,37 @@ def test_facet_edge_cases():
         FacetOne.from_mesh(mesh)(mesh.points.clone().requires_grad_(True))
     with pytest.raises(RuntimeError):
         FacetOne.from_mesh(mesh.to("cpu"))(mesh.points.cpu())
+
+
+@pytest.mark.parametrize("et", ["triangle6c", "tetra10c"])
+def test_facet_load_gradient_wrt_point_data(golden_facet, et):
+    """dL/dg of L = w . b(g) is M w (M the symmetric facet mass matrix): the
+    oracle's point load of w, scaled back per component for vector loads."""
+    g = golden_facet
+    mesh = mesh_of(g, et)
+    pts, el, bd = g[f"{et}/points"], g[f"{et}/elements"], g[f"{et}/boundary"]
+    dim = pts.shape[1]
+    rng = np.random.default_rng(5)
+    g0 = torch.tensor(g[f"{et}/facet_g"], device=DEV)
+
+    field = g0.clone().requires_grad_(True)
+    b = FacetPoint.from_mesh(mesh, quadrature_order=3)(mesh.points, point_data={"g": field})
+    w = rng.normal(size=b.shape[0])
+    (b * torch.tensor(w, device=DEV)).sum().backward()
+    ref = fem.facet_load(pts, el, et.rstrip("c"), bd, 3, "point", w)
+    assert rel_err(field.grad.cpu().numpy(), ref) <= 1e-12
+
+    t = [0.5, -1.0] if dim == 2 else [0.0, 0.3, -1.0]
+
+    class PointTraction(tg.FacetAssembler):
+        def forward(self, v, p):
+            return p * v[:, None] * torch.tensor(t, dtype=v.dtype, device=v.device)
+
+    field = g0.clone().requires_grad_(True)
+    b = PointTraction.from_mesh(mesh, quadrature_order=2)(mesh.points, point_data={"p": field})
+    assert rel_err(b.detach().cpu().numpy(),
+                   fem.facet_load(pts, el, et.rstrip("c"), bd, 2, "point", g0.cpu().numpy()[:, None] * np.array(t))) <= 1e-12
+    W = rng.normal(size=(pts.shape[0], dim))
+    (b * torch.tensor(W.reshape(-1), device=DEV)).sum().backward()
+    ref = fem.facet_load(pts, el, et.rstrip("c"), bd, 2, "point", W @ np.array(t))
+    assert rel_err(field.grad.cpu().numpy(), ref) <= 1e-12
