@@ -117,6 +117,20 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def aggregate_over_ranks(total_ms: float, units: int, device):
+    """(the timed region's duration, max over ranks, in ms; the units all
+    ranks processed, summed).  With one process the inputs come back."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(total_ms), int(units)
+    t = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+    u = torch.tensor([int(units)], dtype=torch.int64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(u.item())
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -234,12 +248,9 @@ def run_ours(args):
     clk = clocks.stop()
     total_ms = t0.elapsed_time(t1)
     kernel_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
-    if world > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(tt)
+    total_ms, units = aggregate_over_ranks(total_ms, E * args.steps, dev)
     ms_per_step = total_ms / args.steps
-    value = world * E / (ms_per_step * 1e-3)
+    value = units / (total_ms * 1e-3)
 
     # ---- float32 variant of the same assembly (secondary line item)
     def time_calls(fn, reps=5):
@@ -430,7 +441,8 @@ def run_ours(args):
         stream.wait_stream(st)
     s1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = s0.elapsed_time(s1) / args.steps
+    e2e_total, e2e_units = aggregate_over_ranks(s0.elapsed_time(s1), E * args.steps, dev)
+    e2e_ms = e2e_total / args.steps
     h2d = pts_h.numel() * 8 + kap_h.numel() * 8
     d2h = nnz * 8
 
@@ -524,7 +536,7 @@ def run_ours(args):
                          "algorithmic_bytes_per_launch": alg, "kernel_ms": kernel_ms,
                          "ncu_issue_active_pct": read_profile_value("smsp__issue_active.avg.pct_of_peak_sustained_active:"),
                          "limiter": "instruction issue (double-float arithmetic on the FP32 pipe), not HBM"},
-            "e2e": {"value": world * E / (e2e_ms * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
+            "e2e": {"value": e2e_units / (e2e_total * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
                     "pipelining": f"consecutive steps on {n_streams} streams in turn"},
             "cpu_baseline": cpu,
