@@ -10,6 +10,7 @@ if ROOT not in sys.path:
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "reference_fem.npz")
 GOLDEN_FACET = os.path.join(ROOT, "tests", "golden", "reference_facet.npz")
+GOLDEN_CONDENSE = os.path.join(ROOT, "tests", "golden", "reference_condense.npz")
 
 
 def pytest_configure(config):
@@ -38,3 +39,8 @@ def golden():
 @pytest.fixture(scope="session")
 def golden_facet():
     return dict(np.load(GOLDEN_FACET))
+
+
+@pytest.fixture(scope="session")
+def golden_condense():
+    return dict(np.load(GOLDEN_CONDENSE))

@@ -262,6 +262,54 @@ def main(ref_root):
     np.savez_compressed(os.path.join(HERE, "reference_fem.npz"), **out)
     print("wrote", len(out), "arrays")
     facet_fixtures(tm, torch, meshes, mk_mesh)
+    condense_fixtures(tm, torch, mk_mesh, canon, EElasticity)
+
+
+def condense_fixtures(tm, torch, mk_mesh, canon, EElasticity):
+    """Condenser with prescribed (nonzero) Dirichlet values, update_dirichlet
+    + condense_rhs, recover; and a small version of the clamped elasticity
+    pipeline (all three dofs fixed on x = 0, body force (0, 0, -1),
+    per-element E), solved with scipy's direct solver."""
+    import scipy.sparse.linalg as spla
+    out = {}
+    pts, cells, bd = square_mesh(8, jitter=0.2, seed=21)
+    mesh = mk_mesh(pts, cells, bd, "triangle")
+    K = tm.LaplaceElementAssembler.from_mesh(mesh, quadrature_order=2)(mesh.points)
+    b = tm.const_node_assembler(1.0).from_mesh(mesh, quadrature_order=2)(mesh.points)
+    g_full = np.sin(2.0 * pts[:, 0]) + pts[:, 1] ** 2
+    cond = tm.Condenser(mesh.boundary_mask, torch.from_numpy(g_full))
+    K_ii, f_i = cond(K, b)
+    c = K_ii.to_scipy_coo().tocsr()
+    c.sum_duplicates()
+    c.sort_indices()
+    u = cond.recover(torch.from_numpy(spla.spsolve(c.tocsc(), f_i.numpy()))).numpy()
+    g2 = np.cos(pts[bd, 0]) - pts[bd, 1]
+    cond.update_dirichlet(torch.from_numpy(g2))
+    f_i2 = cond.condense_rhs(b)
+    u2 = cond.recover(torch.from_numpy(spla.spsolve(c.tocsc(), f_i2.numpy()))).numpy()
+    out.update({"dir/points": pts, "dir/elements": cells, "dir/boundary": bd, "dir/g_full": g_full,
+                "dir/g2_outer": g2, "dir/f_i": f_i.numpy(), "dir/u": u, "dir/f_i2": f_i2.numpy(), "dir/u2": u2})
+
+    pts, cells, bd = cube_mesh(3, jitter=0.15, seed=22)
+    mesh = mk_mesh(pts, cells, bd, "tetra")
+    E = np.exp(0.5 * np.random.default_rng(23).normal(size=cells.shape[0]))
+    K = EElasticity.from_mesh(mesh, quadrature_order=1)(mesh.points, element_data={"E": torch.from_numpy(E)})
+    f = tm.const_node_assembler(torch.tensor([0.0, 0.0, -1.0], dtype=torch.float64)).from_mesh(
+        mesh, quadrature_order=1)(mesh.points)
+    clamp = np.repeat(np.isclose(pts[:, 0], 0.0), 3)
+    cond = tm.Condenser(torch.from_numpy(clamp))
+    K_ii, f_i = cond(K, f)
+    c = K_ii.to_scipy_coo().tocsr()
+    c.sum_duplicates()
+    c.sort_indices()
+    u = cond.recover(torch.from_numpy(spla.spsolve(c.tocsc(), f_i.numpy()))).numpy()
+    ip, ix, dv = canon(K)
+    out.update({"c2/points": pts, "c2/elements": cells, "c2/E": E, "c2/clamp": clamp, "c2/f": f.numpy(),
+                "c2/K_indptr": ip, "c2/K_indices": ix, "c2/K_data": dv,
+                "c2/Kii_indptr": c.indptr.astype(np.int64), "c2/Kii_indices": c.indices.astype(np.int64),
+                "c2/Kii_data": c.data, "c2/f_i": f_i.numpy(), "c2/u": u})
+    np.savez_compressed(os.path.join(HERE, "reference_condense.npz"), **out)
+    print("wrote", len(out), "condense arrays")
 
 
 def facet_fixtures(tm, torch, meshes, mk_mesh):

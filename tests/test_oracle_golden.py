@@ -160,3 +160,38 @@ def test_oracle_facet_selection_includes_interior_facets(golden_facet):
                          "const", 1.0).sum()
     assert abs(tot - (4 + math.sqrt(2))) < 1e-12
     assert abs(g["triangle/facet_const/q2"].sum() - tot) < 1e-12
+
+
+def test_oracle_condenser_with_prescribed_values(golden_condense):
+    """Nonzero Dirichlet values: f_i = f[inner] - K_io u_o, recover writes the
+    values; update_dirichlet + condense_rhs re-condense with new values
+    (operator/condense.py:222-236, 238-309, 388-458)."""
+    g = golden_condense
+    pts, el, bd = g["dir/points"], g["dir/elements"], g["dir/boundary"]
+    ip, ix, dv = fem.assemble_csr(pts, el, "triangle", "laplace", 2)
+    b = fem.assemble_load(pts, el, "triangle", 2, "const", 1.0)
+    for val, f_key, u_key in ((g["dir/g_full"], "dir/f_i", "dir/u"), (g["dir/g2_outer"], "dir/f_i2", "dir/u2")):
+        iptr, ic, iv, f_i = fem.condense(ip, ix, dv, bd, val, b)
+        assert rel_err(f_i, g[f_key]) <= 1e-12
+        u = fem.recover(fem.spsolve(iptr, ic, iv, f_i), bd, val)
+        assert rel_err(u, g[u_key]) <= 1e-10
+
+
+def test_oracle_clamped_elasticity_pipeline(golden_condense):
+    """Per-element-E elasticity, all three dofs clamped on x = 0, body force
+    (0, 0, -1): K, the condensed system and the displacement."""
+    g = golden_condense
+    pts, el, E, clamp = g["c2/points"], g["c2/elements"], g["c2/E"], g["c2/clamp"]
+    ip, ix, dv = fem.assemble_csr(pts, el, "tetra", "elasticity", 1, coef=E)
+    np.testing.assert_array_equal(ip, g["c2/K_indptr"])
+    np.testing.assert_array_equal(ix, g["c2/K_indices"])
+    assert rel_err(dv, g["c2/K_data"]) <= 1e-12
+    f = fem.assemble_load(pts, el, "tetra", 1, "const", [0.0, 0.0, -1.0])
+    assert rel_err(f, g["c2/f"]) <= 1e-12
+    iptr, ic, iv, f_i = fem.condense(ip, ix, dv, clamp, None, f)
+    np.testing.assert_array_equal(iptr, g["c2/Kii_indptr"])
+    np.testing.assert_array_equal(ic, g["c2/Kii_indices"])
+    assert rel_err(iv, g["c2/Kii_data"]) <= 1e-12
+    assert rel_err(f_i, g["c2/f_i"]) <= 1e-12
+    u = fem.recover(fem.spsolve(iptr, ic, iv, f_i), clamp)
+    assert rel_err(u, g["c2/u"]) <= 1e-10
