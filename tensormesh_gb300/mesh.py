@@ -206,6 +206,73 @@ class Mesh:
     def float(self) -> "Mesh":
         return self.to(dtype=torch.float32)
 
+    # -- fields and graph helpers -------------------------------------------------
+    def register_point_data(self, key: str, value: torch.Tensor) -> "Mesh":
+        """Add a per-point field (mesh.py:147-170)."""
+        assert key not in self.point_data, f"the key {key} already exists in point_data"
+        assert value.shape[0] == self.points.shape[0], \
+            f"the first dimension of value should be {self.points.shape[0]}, but got {value.shape[0]}"
+        self.point_data[key] = value
+        return self
+
+    def register_element_data(self, key: str, value) -> "Mesh":
+        """Add a per-element field (mesh.py:172-199): a tensor for a mesh with
+        one default element type, else a dict with one tensor per default type.
+        Stored as ``cell_data[key][element_type]``, the layout the constructor
+        reads from meshio."""
+        t = self.default_element_type
+        if isinstance(value, torch.Tensor):
+            assert isinstance(t, str), "only for homogeneous elements can value be a tensor; pass a dict per type"
+            assert value.shape[0] == self.cells[t].shape[0], \
+                f"the first dimension of value should be {self.cells[t].shape[0]}, but got {value.shape[0]}"
+            value = {t: value}
+        else:
+            assert isinstance(value, dict), "value should be a tensor or a dict of tensors per element type"
+            types = [t] if isinstance(t, str) else t
+            assert set(types) == set(value), f"the keys of value should be {types}, got {list(value)}"
+            for k, v in value.items():
+                assert v.shape[0] == self.cells[k].shape[0], \
+                    f"the first dimension of value should be {self.cells[k].shape[0]}, but got {v.shape[0]}"
+        self.cell_data.setdefault(key, {}).update(value)
+        return self
+
+    def clone(self) -> "Mesh":
+        """A copy whose tensors are clones (the autograd graph through the
+        points and fields is kept; mesh.py:488-502)."""
+        return Mesh(points=self.points.clone(), cells={k: v.clone() for k, v in self.cells.items()},
+                    point_data={k: v.clone() for k, v in self.point_data.items()},
+                    cell_data={k: {t: v.clone() for t, v in per.items()} for k, per in self.cell_data.items()},
+                    field_data={k: v.clone() for k, v in self.field_data.items()}, cell_sets=dict(self.cell_sets))
+
+    def node_adjacency(self, element_type=None):
+        """Node adjacency with ones where two nodes share an element, the
+        diagonal included, as a canonical-CSR ``SparseMatrix`` [N, N]
+        (mesh.py:327-345, adjacency.py:111-145)."""
+        from .plan import node_pattern
+        from .sparse import SparseMatrix
+        els = self.elements(element_type)
+        if isinstance(els, dict):
+            els = list(els.values())
+        else:
+            els = [els]
+        n = self.n_points
+        if len(els) == 1:
+            pat = node_pattern(els[0], n)
+            indptr, indices = pat.indptr, pat.indices
+        else:
+            keys = []
+            for el in els:
+                e = el.long()
+                B = e.shape[1]
+                keys.append((e.unsqueeze(2).expand(-1, B, B) * n + e.unsqueeze(1).expand(-1, B, B)).reshape(-1))
+            uniq = torch.unique(torch.cat(keys), sorted=True)
+            rows = torch.div(uniq, n, rounding_mode="floor")
+            indices = (uniq - rows * n).to(torch.int32)
+            indptr = torch.zeros(n + 1, dtype=torch.int64, device=uniq.device)
+            indptr[1:] = torch.cumsum(torch.bincount(rows, minlength=n), 0)
+        ones = torch.ones(indices.shape[0], dtype=torch.get_default_dtype(), device=indices.device)
+        return SparseMatrix(ones, indptr=indptr, indices=indices, shape=(n, n))
+
     # -- meshio round trip -------------------------------------------------------
     @classmethod
     def from_meshio(cls, mesh, reorder: bool = False) -> "Mesh":

@@ -174,3 +174,38 @@ def test_gmsh_like_mesh_assembles_its_volume_block():
     np.testing.assert_array_equal(K.indptr.cpu().numpy(), ip)
     np.testing.assert_array_equal(K.indices.cpu().numpy(), ix)
     assert np.max(np.abs(K.values.cpu().numpy() - dv)) <= 1e-12 * np.max(np.abs(dv))
+
+
+def test_register_fields_clone_and_node_adjacency():
+    cube, src = gmsh_like_cube()
+    m = tg.Mesh(src)
+    t = torch.arange(m.n_points, dtype=torch.float64)
+    assert m.register_point_data("temp", t) is m and torch.equal(m.point_data["temp"], t)
+    with pytest.raises(AssertionError):
+        m.register_point_data("temp", t)
+    with pytest.raises(AssertionError):
+        m.register_point_data("short", t[:-1])
+    k = torch.rand(m.n_elements, dtype=torch.float64)
+    m.register_element_data("kappa", k)
+    assert torch.equal(m.cell_data["kappa"]["tetra"], k)
+    with pytest.raises(AssertionError):
+        m.register_element_data("bad", k[:-1])
+    pts = m.points.clone().requires_grad_(True)
+    m2 = tg.Mesh(points=pts, cells=m.cells, point_data=m.point_data).clone()
+    m2.points.sum().backward()
+    assert torch.equal(pts.grad, torch.ones_like(pts))
+    # node adjacency: all pairs inside each tetra, diagonal included, canonical order
+    A = m.node_adjacency()
+    el = m.cells["tetra"].numpy()
+    pairs = {(int(a), int(b)) for e in el for a in e for b in e}
+    rows = np.repeat(np.arange(m.n_points), np.diff(A.indptr.numpy()))
+    got = list(zip(rows.tolist(), A.indices.numpy().tolist()))
+    assert got == sorted(pairs)
+    assert A.values.dtype == torch.get_default_dtype() and bool((A.values == 1).all())
+    # several types of one dimension are merged
+    two = tg.Mesh(points=torch.zeros(5, 2), cells={"triangle": torch.tensor([[0, 1, 2]]),
+                                                   "quad": torch.tensor([[1, 2, 3, 4]])})
+    A2 = two.node_adjacency()
+    rows = np.repeat(np.arange(5), np.diff(A2.indptr.numpy()))
+    assert set(zip(rows.tolist(), A2.indices.numpy().tolist())) == (
+        {(a, b) for a in (0, 1, 2) for b in (0, 1, 2)} | {(a, b) for a in (1, 2, 3, 4) for b in (1, 2, 3, 4)})
