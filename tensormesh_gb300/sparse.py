@@ -3,7 +3,9 @@
 Mirrors the accessors of TensorMesh's ``SparseMatrix`` (sparse/matrix.py:
 28-636 on top of ``torch_sla.SparseTensor``): ``values``/``edata``,
 ``row``/``col`` (COO view), ``shape``, ``nnz``, ``@``, ``solve``,
-``to_dense``, ``to_scipy_coo``, ``from_block_coo``, ``layout_signature``.
+``to_dense``, ``to_scipy_coo``, ``from_block_coo``, ``layout_signature``,
+``+``/``-``/scalar ``*``, ``transpose``/``T``, ``degree``, ``from_dense``,
+``eye``.
 
 Storage is CSR (``indptr`` int64, ``indices`` int32) in canonical order:
 rows ascending, columns ascending inside a row.  For scalar forms that is
@@ -118,6 +120,104 @@ class SparseMatrix:
     def diagonal(self) -> torch.Tensor:
         from .solve import csr_diagonal
         return csr_diagonal(self)
+
+    @property
+    def grad(self) -> Optional["SparseMatrix"]:
+        """The gradient of the values as a matrix of the same pattern, or None."""
+        g = self.values.grad
+        return None if g is None else self.with_values(g)
+
+    def detach(self) -> "SparseMatrix":
+        return self.with_values(self.values.detach())
+
+    def cpu(self) -> "SparseMatrix":
+        return self.to("cpu")
+
+    def cuda(self, device=None) -> "SparseMatrix":
+        return self.to("cuda" if device is None else device)
+
+    def degree(self, axis: int = 0) -> torch.Tensor:
+        """Entries per row (axis 0) or per column (axis 1) (matrix.py:213-229)."""
+        if axis == 0:
+            return self.indptr[1:] - self.indptr[:-1]
+        return torch.bincount(self.col, minlength=self.shape[1])
+
+    def transpose(self) -> "SparseMatrix":
+        """A^T in canonical CSR (matrix.py:231-243); differentiable in the values."""
+        return SparseMatrix(self.values, self.col, self.row, (self.shape[1], self.shape[0]))
+
+    @property
+    def T(self) -> "SparseMatrix":
+        return self.transpose()
+
+    # -- arithmetic (matrix.py:154-178): on the values, so autograd flows ------
+    def _same_pattern(self, other: "SparseMatrix") -> bool:
+        if self.shape != other.shape or self.nnz != other.nnz:
+            return False
+        return self.has_same_layout(other) or (
+            torch.equal(self.indptr, other.indptr.to(self.indptr.device)) and
+            torch.equal(self.indices, other.indices.to(self.indices.device)))
+
+    def __add__(self, other):
+        if isinstance(other, SparseMatrix):
+            assert self.shape == other.shape, f"shape mismatch {self.shape} vs {other.shape}"
+            ov = other.values.to(device=self.device, dtype=self.dtype)
+            if self._same_pattern(other):
+                return self.with_values(self.values + ov)
+            # union of the two patterns; a position holds at most one entry of
+            # each operand, so the sum does not depend on the order of the adds
+            return SparseMatrix(torch.cat([self.values, ov]), torch.cat([self.row, other.row.to(self.device)]),
+                                torch.cat([self.col, other.col.to(self.device)]), self.shape)
+        if isinstance(other, (int, float)) and other == 0:
+            return self
+        return NotImplemented
+
+    __radd__ = __add__
+
+    def __neg__(self) -> "SparseMatrix":
+        return self.with_values(-self.values)
+
+    def __sub__(self, other):
+        if isinstance(other, SparseMatrix):
+            return self + (-other)
+        if isinstance(other, (int, float)) and other == 0:
+            return self
+        return NotImplemented
+
+    def __rsub__(self, other):
+        if isinstance(other, (int, float)) and other == 0:
+            return -self
+        return NotImplemented
+
+    def __mul__(self, other):
+        if isinstance(other, SparseMatrix):
+            if not self._same_pattern(other):
+                raise NotImplementedError("elementwise product of matrices with different patterns")
+            return self.with_values(self.values * other.values.to(device=self.device, dtype=self.dtype))
+        if isinstance(other, (int, float)) or (torch.is_tensor(other) and other.dim() == 0):
+            return self.with_values(self.values * other)
+        return NotImplemented
+
+    __rmul__ = __mul__
+
+    def __truediv__(self, other):
+        if isinstance(other, (int, float)) or (torch.is_tensor(other) and other.dim() == 0):
+            return self.with_values(self.values / other)
+        return NotImplemented
+
+    @staticmethod
+    def from_dense(tensor: torch.Tensor) -> "SparseMatrix":
+        """The nonzero entries of a dense 2-D tensor (matrix.py:309-324)."""
+        assert tensor.dim() == 2, f"a 2-D tensor is required, got {tuple(tensor.shape)}"
+        r, c = torch.nonzero(tensor, as_tuple=True)
+        return SparseMatrix(tensor[r, c], r, c, tuple(tensor.shape))
+
+    @staticmethod
+    def eye(n: int, value: float = 1.0, dtype=None, device=None) -> "SparseMatrix":
+        """value * I (matrix.py:439-459)."""
+        i = torch.arange(n, device=device)
+        v = torch.full((n,), value, dtype=dtype or torch.get_default_dtype(), device=device)
+        return SparseMatrix(v, i, i, (n, n))
 
     # -- operators -------------------------------------------------------------
     def __matmul__(self, x: torch.Tensor) -> torch.Tensor:
