@@ -147,7 +147,27 @@ def launch_assemble(topo: MeshTopology, form_code: int, points: torch.Tensor, ou
     return tables  # keep alive until the stream consumes it
 
 
-class ElementAssembler(nn.Module):
+class _AssemblerDevice:
+    """``device`` / ``dtype`` / ``type(dtype)`` of the reference assemblers
+    (element_assembler.py:172-194, node_assembler.py): the stored points
+    carry both; ``type`` casts them (float32 or float64)."""
+
+    @property
+    def device(self) -> torch.device:
+        return self.points.device
+
+    @property
+    def dtype(self) -> torch.dtype:
+        return self.points.dtype
+
+    def type(self, dtype: torch.dtype):
+        if dtype not in (torch.float32, torch.float64):
+            raise TypeError(f"the dtype {dtype} is not supported (float32 or float64)")
+        self.points = self.points.to(dtype)
+        return self
+
+
+class ElementAssembler(_AssemblerDevice, nn.Module):
     """Assemble a bilinear form into a global CSR matrix on the GPU."""
 
     _builtin_form: Optional[F_.BilinearForm] = None
@@ -350,7 +370,7 @@ class LinearElasticityElementAssembler(ElementAssembler):
     _builtin_form = F_.BilinearForm("elasticity", None)
 
 
-class NodeAssembler(nn.Module):
+class NodeAssembler(_AssemblerDevice, nn.Module):
     """Assemble a linear form into a node vector on the GPU."""
 
     precision = "emulated"
