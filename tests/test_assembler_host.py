@@ -24,3 +24,21 @@ def test_from_assembler_shares_topology_and_calls_post_init():
     assert (b.E, b.nu) == (3.0, 0.25)
     with pytest.raises(AssertionError):
         tg.LaplaceElementAssembler.from_assembler(object())
+
+
+def test_facet_topology_groups_pairs_by_node_in_order():
+    """The (selected facet, cell node) pairs of a FacetTopology are grouped by
+    node, in pair order inside a node (the fixed order of the reduction)."""
+    from tensormesh_gb300.facet import FacetTopology
+    from oracle import fem
+    mesh = tg.Mesh.gen_unit_cube(3).to_p2()
+    el = mesh.cells["tetra10"]
+    topo = FacetTopology(el, mesh.n_points, "tetra10", mesh.boundary_mask)
+    e, f = fem.facet_select(el.numpy(), "tetra10", mesh.boundary_mask.numpy())
+    assert torch.equal(topo.sel, torch.from_numpy(e * 4 + f))
+    nodes = el[torch.from_numpy(e)].reshape(-1)
+    for n in range(mesh.n_points):
+        group = topo.perm[topo.ptr[n]:topo.ptr[n + 1]]
+        assert bool((nodes[group] == n).all())
+        assert bool((group[1:] > group[:-1]).all())
+    assert int(topo.ptr[-1]) == nodes.numel()
