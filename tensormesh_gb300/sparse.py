@@ -21,7 +21,6 @@ from typing import Optional, Tuple
 import numpy as np
 import torch
 
-from . import _lib
 
 
 class SparseMatrix:

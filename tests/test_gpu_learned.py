@@ -4,7 +4,6 @@ network on the CPU (same bf16 rounding points), and what the trained network
 gains inside flexible PCG over the same method without it."""
 import math
 
-import numpy as np
 import pytest
 import torch
 

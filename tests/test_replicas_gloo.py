@@ -4,7 +4,6 @@ ranks (the multi-GPU run is replicas only: no data-path collective)."""
 import os
 import socket
 
-import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 

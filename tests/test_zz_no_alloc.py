@@ -8,7 +8,6 @@ fails, a run that stops at the first failure has already run every other
 test.  It is self-contained, so it also passes alone in a fresh process."""
 import ctypes
 
-import numpy as np
 import pytest
 import torch
 
