@@ -434,30 +434,33 @@ int launch_patch_assemble(const tm_patch_plan& plan, const tm_assemble_args& arg
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
 
-// Dispatch over form/H/precision for one element type (instantiated in one
-// translation unit per element so the build parallelises).
-template <int EL>
-int assemble_element(const tm_patch_plan& plan, const tm_assemble_args& a, cudaStream_t s) {
+// Dispatch over form/H for one element type and one arithmetic (T stored,
+// R computed in).  The element types instantiate it in their own translation
+// units (the heaviest element splits it per arithmetic) so the build
+// parallelises.
+template <int EL, class T, class R>
+int assemble_element_as(const tm_patch_plan& plan, const tm_assemble_args& a, cudaStream_t s) {
   constexpr int D = Elem<EL>::D;
-#define TM_PREC_DISPATCH(FORM, H)                                                         \
-  do {                                                                                    \
-    if (a.dtype == TM_F32) return launch_patch_assemble<EL, FORM, H, float, float>(plan, a, s); \
-    if (a.precision == TM_PREC_NATIVE)                                                    \
-      return launch_patch_assemble<EL, FORM, H, double, double>(plan, a, s);             \
-    return launch_patch_assemble<EL, FORM, H, double, df64>(plan, a, s);                 \
-  } while (0)
   switch (a.form) {
-    case TM_FORM_LAPLACE: TM_PREC_DISPATCH(TM_FORM_LAPLACE, 1);
-    case TM_FORM_MASS: TM_PREC_DISPATCH(TM_FORM_MASS, 1);
-    case TM_FORM_ELASTICITY: TM_PREC_DISPATCH(TM_FORM_ELASTICITY, D);
+    case TM_FORM_LAPLACE: return launch_patch_assemble<EL, TM_FORM_LAPLACE, 1, T, R>(plan, a, s);
+    case TM_FORM_MASS: return launch_patch_assemble<EL, TM_FORM_MASS, 1, T, R>(plan, a, s);
+    case TM_FORM_ELASTICITY: return launch_patch_assemble<EL, TM_FORM_ELASTICITY, D, T, R>(plan, a, s);
     case TM_FORM_LOAD:
-      if (a.n_comp == 1) TM_PREC_DISPATCH(TM_FORM_LOAD, 1);
-      if (a.n_comp == 2) TM_PREC_DISPATCH(TM_FORM_LOAD, 2);
-      if (a.n_comp == 3) TM_PREC_DISPATCH(TM_FORM_LOAD, 3);
+      if (a.n_comp == 1) return launch_patch_assemble<EL, TM_FORM_LOAD, 1, T, R>(plan, a, s);
+      if (a.n_comp == 2) return launch_patch_assemble<EL, TM_FORM_LOAD, 2, T, R>(plan, a, s);
+      if (a.n_comp == 3) return launch_patch_assemble<EL, TM_FORM_LOAD, 3, T, R>(plan, a, s);
       return TM_ERR_UNSUPPORTED;
     default: return TM_ERR_UNSUPPORTED;
   }
-#undef TM_PREC_DISPATCH
+}
+
+// float32 in float; float64 in native FP64 (precision "native") or in
+// double-float (the default).
+template <int EL>
+int assemble_element(const tm_patch_plan& plan, const tm_assemble_args& a, cudaStream_t s) {
+  if (a.dtype == TM_F32) return assemble_element_as<EL, float, float>(plan, a, s);
+  if (a.precision == TM_PREC_NATIVE) return assemble_element_as<EL, double, double>(plan, a, s);
+  return assemble_element_as<EL, double, df64>(plan, a, s);
 }
 
 }  // namespace tmg

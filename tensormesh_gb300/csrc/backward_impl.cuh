@@ -380,27 +380,30 @@ int launch_patch_backward(const tm_patch_plan& plan, const tm_assemble_args& arg
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
 
-template <int EL>
-int backward_element(const tm_patch_plan& plan, const tm_assemble_args& a, const tm_backward_args& bw,
-                     cudaStream_t s) {
+// Dispatch over form/H for one element type and one value type (computed in
+// the same type).
+template <int EL, class T>
+int backward_element_as(const tm_patch_plan& plan, const tm_assemble_args& a, const tm_backward_args& bw,
+                        cudaStream_t s) {
   constexpr int D = Elem<EL>::D;
-#define TM_BW(FORM, H)                                                                               \
-  do {                                                                                               \
-    if (a.dtype == TM_F32) return launch_patch_backward<EL, FORM, H, float, float>(plan, a, bw, s); \
-    return launch_patch_backward<EL, FORM, H, double, double>(plan, a, bw, s);                      \
-  } while (0)
   switch (a.form) {
-    case TM_FORM_LAPLACE: TM_BW(TM_FORM_LAPLACE, 1);
-    case TM_FORM_MASS: TM_BW(TM_FORM_MASS, 1);
-    case TM_FORM_ELASTICITY: TM_BW(TM_FORM_ELASTICITY, D);
+    case TM_FORM_LAPLACE: return launch_patch_backward<EL, TM_FORM_LAPLACE, 1, T, T>(plan, a, bw, s);
+    case TM_FORM_MASS: return launch_patch_backward<EL, TM_FORM_MASS, 1, T, T>(plan, a, bw, s);
+    case TM_FORM_ELASTICITY: return launch_patch_backward<EL, TM_FORM_ELASTICITY, D, T, T>(plan, a, bw, s);
     case TM_FORM_LOAD:
-      if (a.n_comp == 1) TM_BW(TM_FORM_LOAD, 1);
-      if (a.n_comp == 2) TM_BW(TM_FORM_LOAD, 2);
-      if (a.n_comp == 3) TM_BW(TM_FORM_LOAD, 3);
+      if (a.n_comp == 1) return launch_patch_backward<EL, TM_FORM_LOAD, 1, T, T>(plan, a, bw, s);
+      if (a.n_comp == 2) return launch_patch_backward<EL, TM_FORM_LOAD, 2, T, T>(plan, a, bw, s);
+      if (a.n_comp == 3) return launch_patch_backward<EL, TM_FORM_LOAD, 3, T, T>(plan, a, bw, s);
       return TM_ERR_UNSUPPORTED;
     default: return TM_ERR_UNSUPPORTED;
   }
-#undef TM_BW
+}
+
+template <int EL>
+int backward_element(const tm_patch_plan& plan, const tm_assemble_args& a, const tm_backward_args& bw,
+                     cudaStream_t s) {
+  if (a.dtype == TM_F32) return backward_element_as<EL, float>(plan, a, bw, s);
+  return backward_element_as<EL, double>(plan, a, bw, s);
 }
 
 }  // namespace tmg
