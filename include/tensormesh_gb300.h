@@ -330,10 +330,12 @@ int tm_pcg_result(const void* work, int32_t* iters, double* res, double* bnorm, 
  * scratch in a 32 MiB array inside this library (reserved on every GPU that
  * loads it, until exit), so the caller passes only A, b and x.
  * Limits and rules: n <= 1,000,000 rows, else TM_ERR_INDEX; calls share the
- * array, so calls that overlap on the GPU race and must be serialised; the
- * first call on a device looks up the array's address and should come before
- * any stream capture; the call synchronises `stream` and returns the solve
- * status (as tm_pcg_result) with the iteration count and recurrence residual.
+ * array, so calls that overlap on the GPU race and must be serialised; every
+ * call looks up the array's address on the current device (no allocation);
+ * the call synchronises `stream` to read the result, so it cannot run on a
+ * stream that is being captured (TM_ERR_INVALID, nothing launched); it
+ * returns the solve status (as tm_pcg_result) with the iteration count and
+ * recurrence residual, which are set to 0 before any early return.
  */
 int tm_pcg_jacobi_noalloc(int64_t n, const int64_t* indptr, const int32_t* indices, const float* values,
                           const float* b, float* x, double rtol, double atol, int32_t maxiter, int32_t* out_iters,

@@ -14,7 +14,8 @@ from .assemble import (ElementAssembler, NodeAssembler, LaplaceElementAssembler,
 from .condense import Condenser
 from .energy import NeoHookeanModel
 from .facet import FacetAssembler
+from .validate import set_input_checks
 
 __all__ = ["Mesh", "SparseMatrix", "ElementAssembler", "NodeAssembler", "LaplaceElementAssembler",
            "MassElementAssembler", "LinearElasticityElementAssembler", "const_node_assembler",
-           "func_node_assembler", "Condenser", "NeoHookeanModel", "FacetAssembler"]
+           "func_node_assembler", "Condenser", "NeoHookeanModel", "FacetAssembler", "set_input_checks"]

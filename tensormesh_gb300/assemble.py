@@ -33,6 +33,7 @@ import torch.nn as nn
 from . import _lib, element as E_, forms as F_
 from .plan import PatchPlan, block_pattern, node_pattern
 from .sparse import SparseMatrix
+from .validate import check_connectivity
 
 PRECISION = {"emulated": _lib.TM_PREC_EMULATED, "native": _lib.TM_PREC_NATIVE}
 
@@ -44,6 +45,10 @@ class MeshTopology:
     def __init__(self, elements: torch.Tensor, points: torch.Tensor, element_type: str):
         self.element_type = element_type
         self.el_id, self.dim, self.n_basis, _ = E_.element_info(element_type)
+        assert elements.dim() == 2, f"the connectivity should be [n_element, n_basis], but got {tuple(elements.shape)}"
+        assert elements.shape[1] == self.n_basis, \
+            f"{element_type} elements have {self.n_basis} nodes, but the connectivity has {elements.shape[1]} columns"
+        check_connectivity(elements, int(points.shape[0]))
         self.elements = elements.to(torch.int32).contiguous()
         self._elements_long = elements.long()
         self.n_points = int(points.shape[0])
@@ -410,6 +415,26 @@ class NodeAssembler(_AssemblerDevice, nn.Module):
 
     def forward(self, *args):
         raise NotImplementedError("subclass NodeAssembler and define forward(...)")
+
+    # The reference's fast mode (assemble/node_assembler.py:416-536) swaps its
+    # vmap path for broadcast operations, optionally under torch.compile.  The
+    # load here is always one fused kernel launch, so these switches only
+    # record the request; ``compile`` never calls torch.compile.
+    def compile(self, mode: str = "disable", fullgraph: bool = False, dynamic=None, backend: str = "inductor",
+                **kwargs) -> "NodeAssembler":
+        """Accepted for drop-in use; returns ``self`` (the kernel path is already the fast path)."""
+        self._compile_request = dict(mode=mode, fullgraph=fullgraph, dynamic=dynamic, backend=backend, **kwargs)
+        return self
+
+    def flat_mode(self) -> "NodeAssembler":
+        return self.compile(mode="disable")
+
+    def reset_compile(self) -> "NodeAssembler":
+        self._compile_request = None
+        return self
+
+    def is_compiled(self) -> bool:
+        return getattr(self, "_compile_request", None) is not None
 
     def _resolve_form(self, fn, point_data, scalar_data) -> F_.LinearForm:
         fn = self.forward if fn is None else fn

@@ -7,6 +7,7 @@ import torch
 from . import _lib
 from . import element as E_
 from .sparse import SparseMatrix
+from .validate import check_finite
 
 _FORM_CODE = {"laplace": _lib.TM_FORM_LAPLACE, "mass": _lib.TM_FORM_MASS, "elasticity": _lib.TM_FORM_ELASTICITY}
 
@@ -32,6 +33,7 @@ def assemble_matrix(asm, form, points, element_data, point_data, scalar_data) ->
     H = topo.dim if form.kind == "elasticity" else 1
     dptr, dind = topo.dof_pattern(H)
     kind, coef, scal = _coefficient(form, points, element_data, point_data, scalar_data)
+    check_finite((("points", points), ("the coefficient", coef)))
     pts = points.detach().contiguous()
     out = torch.empty(dind.shape[0], dtype=points.dtype, device=points.device)
     from .adjoint import needs_grad, AssembleMatrixFn
@@ -100,6 +102,7 @@ def _dtype(t):
 def assemble_load(asm, form, points, point_data, scalar_data) -> torch.Tensor:
     topo = asm.topology
     kind, coef, scal, H = _load_coefficient(asm, form, points, point_data, scalar_data)
+    check_finite((("points", points), ("the load coefficient", coef)))
     from .adjoint import needs_grad, AssembleLoadFn
     if needs_grad(points, coef):
         out = AssembleLoadFn.apply(points, coef, asm, kind, tuple(scal), H)

@@ -75,15 +75,21 @@ class Condenser(nn.Module):
         self.n_inner_dof = self.n_dof - self.n_outer_dof
 
     def _normalize_value(self, value):
+        """Prescribed values on the Dirichlet dofs only (condense.py:167-180
+        accepts the same two layouts).  ``None`` means homogeneous; a vector
+        over all dofs is restricted through the mask; a vector already over
+        the Dirichlet dofs passes through.  Anything else is an
+        AssertionError, as in the reference."""
         mask = self.dirichlet_mask
-        n_outer = int(mask.sum())
+        n_all, n_fixed = int(mask.shape[0]), int(mask.sum())
         if value is None:
-            return torch.zeros(n_outer, device=mask.device)
-        assert value.ndim == 1, f"dirichlet_value must be 1D, got shape {tuple(value.shape)}"
-        if value.shape[0] == mask.shape[0]:
+            return torch.zeros(n_fixed, device=mask.device)
+        assert value.ndim == 1, f"expected a 1-D dirichlet_value, got {value.ndim}-D {tuple(value.shape)}"
+        length = int(value.shape[0])
+        assert length in (n_all, n_fixed), \
+            f"dirichlet_value has {length} entries; expected {n_all} (every dof) or {n_fixed} (Dirichlet dofs)"
+        if length == n_all and n_all != n_fixed:
             return value[mask.to(value.device)]
-        assert value.shape[0] == n_outer, (f"dirichlet_value must have length n_dof ({mask.shape[0]}) "
-                                           f"or n_outer_dof ({n_outer}), got {value.shape[0]}")
         return value
 
     def update_dirichlet(self, dirichlet_value: torch.Tensor):

@@ -560,6 +560,7 @@ static int launch_pcg(int64_t n, const int64_t* indptr, const int32_t* indices, 
   T* partials = base + 6 * n;
   if (cudaMemsetAsync(st, 0, sizeof(tmg::PcgState), s) != cudaSuccess) return TM_ERR_CUDA;
   tmg::diag_inv_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, indptr, indices, values, dinv);
+  if (cudaPeekAtLastError() != cudaSuccess) return TM_ERR_CUDA;
   const T* cdinv = dinv;
   void* args[] = {(void*)&n, (void*)&indptr, (void*)&indices, (void*)&values, (void*)&cdinv, (void*)&b, (void*)&x,
                   (void*)&r, (void*)&z, (void*)&p0, (void*)&p1, (void*)&q, (void*)&partials, (void*)&st,
@@ -582,6 +583,7 @@ static int launch_pcg_df64(int64_t n, const int64_t* indptr, const int32_t* indi
   double* partials = reinterpret_cast<double*>(val + nnz);
   if (cudaMemsetAsync(st, 0, sizeof(tmg::PcgState), s) != cudaSuccess) return TM_ERR_CUDA;
   if (nnz > 0) tmg::split_kernel<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(nnz, values, val);
+  if (cudaPeekAtLastError() != cudaSuccess) return TM_ERR_CUDA;
   const tmg::F2* cval = val;
   void* args[] = {(void*)&n, (void*)&indptr, (void*)&indices, (void*)&cval, (void*)&b, (void*)&x, (void*)&xv,
                   (void*)&r, (void*)&z, (void*)&p0, (void*)&p1, (void*)&q, (void*)&dinv, (void*)&partials,
@@ -702,8 +704,8 @@ extern "C" int tm_condense_rhs(int32_t dtype, int64_t n_inner, const int64_t* in
 // allocation afterwards (embedded / real-time deployments), a plugin that
 // receives its vectors from a host framework owning the only allocator, or a
 // solve issued while that framework's memory pool is exhausted.  For them
-// tm_pcg_jacobi_noalloc keeps the solver's scratch (state word, five vectors,
-// reduction partials) in a fixed array that lives in this library's own
+// tm_pcg_jacobi_noalloc keeps the solver's scratch (state word, six vectors
+// dinv, r, z, p0, p1, q, and the reduction partials) in a fixed array that lives in this library's own
 // device memory, so the caller passes only the matrix, b and x.
 //
 // The array is kTmNoAllocScratchBytes (32 MiB) on every GPU that loads the
@@ -712,39 +714,36 @@ extern "C" int tm_condense_rhs(int32_t dtype, int64_t n_inner, const int64_t* in
 // different host threads, on one device) race on it and must be serialised
 // by the caller.  The solver state at its start is cleared on every call.
 // Limit: n <= kTmNoAllocMaxRows rows (the vectors must fit the array).
-// The first call on a device looks up the array's device address
-// (cudaGetSymbolAddress, with that device current); make that first call
-// before any stream capture.  The call synchronises its stream to read the
-// result back.
+// Every call looks up the array's device address on the current device
+// (cudaGetSymbolAddress, a host-side query that allocates nothing), so the
+// address stays valid across a cudaDeviceReset.  The call synchronises its
+// stream to read the result back, so it cannot be issued while that stream
+// is being captured into a CUDA graph: a capturing stream is rejected with
+// TM_ERR_INVALID before anything is launched.
 // ---------------------------------------------------------------------------
 constexpr size_t kTmNoAllocScratchBytes = size_t(32) << 20;
 constexpr int64_t kTmNoAllocMaxRows = 1000000;
 static __device__ __align__(256) unsigned char tm_pcg_noalloc_scratch[kTmNoAllocScratchBytes];
 
-#include <mutex>
-static std::mutex g_noalloc_mutex;
-static void* g_noalloc_ptr[64] = {nullptr};
-
 static int noalloc_scratch(void** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TM_ERR_CUDA;
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, tm_pcg_noalloc_scratch) != cudaSuccess || !p) return TM_ERR_CUDA;
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, tm_pcg_noalloc_scratch) != cudaSuccess || !p) return TM_ERR_CUDA;
+  *out = p;
   return TM_OK;
 }
 
 extern "C" int tm_pcg_jacobi_noalloc(int64_t n, const int64_t* indptr, const int32_t* indices, const float* values,
                                      const float* b, float* x, double rtol, double atol, int32_t maxiter,
                                      int32_t* out_iters, double* out_res, void* stream) {
+  if (out_iters) *out_iters = 0;
+  if (out_res) *out_res = 0.0;
   if (n < 0 || maxiter < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   if (!indptr || !indices || !values || !b || !x) return TM_ERR_INVALID;
   if (n > kTmNoAllocMaxRows) return TM_ERR_INDEX;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap) != cudaSuccess) return TM_ERR_CUDA;
+  if (cap != cudaStreamCaptureStatusNone) return TM_ERR_INVALID;
   const int nb = tm_pcg_max_blocks(TM_F32);
   if (nb <= 0) return TM_ERR_CUDA;
   if (tm_pcg_workspace_bytes(TM_F32, n, 0, nb) > (int64_t)kTmNoAllocScratchBytes) return TM_ERR_INDEX;

@@ -63,10 +63,30 @@ class _SpMV(torch.autograd.Function):
         if ctx.needs_input_grad[0]:
             gv = g[A.row] * x[A.col]
         if ctx.needs_input_grad[1]:
-            # A^T g via the transpose pattern is not stored; K is typically
-            # symmetric, but stay general with a scatter
-            gx = torch.zeros_like(x).index_add_(0, A.col, values * g[A.row])
+            # A^T g = per column c, the sum over its entries k of values[k] g[row[k]],
+            # reduced in a fixed (row-ascending) order by tm_segment_sum so the
+            # gradient is bitwise repeatable (no atomics)
+            from .adjoint import segment_sum
+            ptr, perm = _column_order(A)
+            prod = (values.detach() * g[A.row]).contiguous()
+            gx = segment_sum(ptr, perm, prod, 1).view(-1)[: A.shape[1]]
         return gv, gx, None
+
+
+def _column_order(A):
+    """CSC view of A's pattern: column pointer and the CSR positions of every
+    column's entries in ascending row order (cached on the matrix)."""
+    cached = getattr(A, "_csc", None)
+    if cached is not None:
+        return cached
+    col = A.col
+    ncol = A.shape[1]
+    perm = torch.argsort(col * max(1, A.shape[0]) + A.row)
+    counts = torch.bincount(col, minlength=ncol)
+    ptr = torch.zeros(ncol + 1, dtype=torch.int64, device=col.device)
+    ptr[1:] = torch.cumsum(counts, 0)
+    A._csc = (ptr, perm)
+    return A._csc
 
 
 def spmv(A, x: torch.Tensor) -> torch.Tensor:

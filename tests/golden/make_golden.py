@@ -379,4 +379,6 @@ def facet_fixtures(tm, torch, meshes, mk_mesh):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the TensorMesh source tree>")
+    main(sys.argv[1])
