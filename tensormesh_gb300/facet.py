@@ -20,12 +20,15 @@ basis values there, zero up to rounding).
 The GPU path covers integrands that are a coefficient times ``v``: a
 constant (scalar or vector), a function of ``x``, or a ``point_data`` field
 (with a constant factor).  One kernel (``tm_facet_load``) integrates every
-selected facet with a float64 facet rule; a fixed-order segment sum reduces
-the per-(facet, node) values to the nodes, so the result is bitwise
+selected facet with the facet rule's tables in float64; a fixed-order segment sum
+reduces the per-(facet, node) values to the nodes, so the result is bitwise
 reproducible.  The reference builds its facet rule in float32
 (element/transformation.py:519-531 keeps get_facet_quadrature's float32
 default), so its float64 facet loads carry float32 rounding of the points
-and weights (about 3e-7 relative); the rule here is exact in float64.
+and weights (about 3e-7 relative against the exact rule).  The default
+``facet_rule="reference"`` uses that same float32 rule, so the loads agree
+with the reference's to rounding; ``facet_rule="exact"`` integrates with the
+float64 rule.
 Gradients flow to the ``point_data`` field of a point-data integrand (the load is
 linear in it with a symmetric facet mass matrix); gradients with respect to
 the points are not provided.
@@ -78,9 +81,20 @@ def facet_rule(dim: int, order: int):
     return E_.quadrature("triangle", order)
 
 
+FACET_RULES = ("reference", "exact")
+
+
 @functools.lru_cache(maxsize=None)
-def facet_tables(element_type: str, order: int):
+def facet_tables(element_type: str, order: int, rule: str = "reference"):
     """(w [F, Qf], N [F, Qf, B], Tc [F, Qf, D-1, B], xi [F, Qf, D]) in float64.
+
+    ``rule="reference"`` (the default) reproduces the reference's facet rule,
+    which it builds in float32 (transformation.py:519-531 keeps
+    get_facet_quadrature's float32 default): the weights are the float32
+    roundings of the exact weights, and the points (where the shape values
+    N are evaluated) are the reference's own float32 points
+    (``facet_reference_points``).  The facet tangents Tc stay exact, as in the
+    reference's facet Jacobian.  ``rule="exact"`` keeps the float64 rule.
 
     Facet f is the affine image r -> P_a + sum_k r_k (P_{v_k} - P_a) of the
     reference segment / triangle (P the reference simplex's vertices, (a, v_1,
@@ -89,30 +103,38 @@ def facet_tables(element_type: str, order: int):
     coordinates.  Tc[f][q][k][b] = grad N_b(xi_fq) . (P_{v_k} - P_a), so the
     physical facet tangents are t_k = sum_b Tc[..][k][b] X_b and the facet
     measure |F| = sqrt(det(t t^T)) (transformation.py:993-1003 detF)."""
+    if rule not in FACET_RULES:
+        raise ValueError(f"facet_rule should be one of {FACET_RULES}, but got {rule!r}")
     _, dim, _, _ = E_.element_info(element_type)
     P = np.concatenate([np.zeros((1, dim)), np.eye(dim)], 0)
     w, r = facet_rule(dim, order)
+    if rule == "reference":
+        from .facet_reference_points import POINTS
+        w = w.astype(np.float32).astype(np.float64)
+        ref_pts = np.array(POINTS[("triangle" if dim == 2 else "tetra", order)], dtype=np.float64)
     W, NN, TT, XI = [], [], [], []
-    for vs in FACET_VERTICES[dim]:
+    for f, vs in enumerate(FACET_VERTICES[dim]):
         T = np.stack([P[v] - P[vs[0]] for v in vs[1:]], 0)           # [D-1, D]
         xi = P[vs[0]][None, :] + r @ T                                 # [Qf, D]
-        N, dN = E_.shape_tables(element_type, xi)                      # [Qf, B], [Qf, B, D]
+        _, dN = E_.shape_tables(element_type, xi)                      # [Qf, B, D]
+        xi_n = ref_pts[f] if rule == "reference" else xi
+        N, _ = E_.shape_tables(element_type, xi_n)                     # [Qf, B]
         W.append(w)
         NN.append(N)
         TT.append(np.einsum("ki,qbi->qkb", T, dN))
-        XI.append(xi)
+        XI.append(xi_n)
     return np.stack(W), np.stack(NN), np.stack(TT), np.stack(XI)
 
 
 _DEVICE_TABLES: Dict[tuple, torch.Tensor] = {}
 
 
-def facet_kernel_tables(element_type: str, order: int, device) -> torch.Tensor:
+def facet_kernel_tables(element_type: str, order: int, device, rule: str = "reference") -> torch.Tensor:
     """Flat float64 [w, N, Tc] as tm_facet_load reads it (cached per device)."""
-    key = (element_type, order, str(torch.device(device)))
+    key = (element_type, order, str(torch.device(device)), rule)
     t = _DEVICE_TABLES.get(key)
     if t is None:
-        w, N, Tc, _ = facet_tables(element_type, order)
+        w, N, Tc, _ = facet_tables(element_type, order, rule)
         flat = np.concatenate([w.ravel(), N.ravel(), Tc.ravel()])
         t = _DEVICE_TABLES[key] = torch.from_numpy(flat).to(device=device, dtype=torch.float64)
     return t
@@ -235,7 +257,13 @@ def recognise_facet(fn, n_basis: int, dim: int, point_shapes: Dict[str, tuple]) 
 
 
 class FacetAssembler(nn.Module):
-    """Assemble a facet (boundary) integrand into a node vector on the GPU."""
+    """Assemble a facet (boundary) integrand into a node vector on the GPU.
+
+    ``facet_rule`` (class attribute, settable per instance): "reference"
+    (default) integrates with the reference's float32-built facet rule, so the
+    loads match the reference's to rounding; "exact" uses the float64 rule."""
+
+    facet_rule = "reference"
 
     def __init__(self, topology: FacetTopology, points: torch.Tensor, quadrature_order: int, *args, **kwargs):
         super().__init__()
@@ -354,8 +382,8 @@ def facet_load(asm: FacetAssembler, form: FacetForm, pts: torch.Tensor, point_da
     if S == 0:
         return torch.zeros(topo.n_points * H, dtype=dtype, device=dev)
     pts = pts.detach().contiguous()
-    tables = facet_kernel_tables(topo.element_type, asm.quadrature_order, dev)
-    Qf = int(facet_tables(topo.element_type, asm.quadrature_order)[0].shape[1])
+    tables = facet_kernel_tables(topo.element_type, asm.quadrature_order, dev, asm.facet_rule)
+    Qf = int(facet_tables(topo.element_type, asm.quadrature_order, asm.facet_rule)[0].shape[1])
     stream = _lib.stream_handle(dev)
     code = _dtype_code(dtype)
     scal, coef = None, None

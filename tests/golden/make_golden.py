@@ -376,6 +376,39 @@ def facet_fixtures(tm, torch, meshes, mk_mesh):
             out[f"facet_table/{key}/q{q}/p"] = p.numpy().astype(np.float64)
     np.savez_compressed(os.path.join(HERE, "reference_facet.npz"), **out)
     print("wrote", len(out), "facet arrays")
+    write_facet_point_module(out)
+
+
+FACET_MODULE = os.path.join(os.path.dirname(os.path.dirname(HERE)), "tensormesh_gb300", "facet_reference_points.py")
+
+
+def write_facet_point_module(arrays, path=FACET_MODULE):
+    """Write the package's table of the reference's float32 facet quadrature
+    points (``facet_table/<family>/q<order>/p`` of the facet fixture), as
+    exact float32 hex literals."""
+    lines = ['"""Facet quadrature points of the reference facet rule, in cell reference',
+             'coordinates, as the reference computes them in float32 (its float32',
+             'least-squares facet maps evaluated in float32; element/element.py:1058-1066,',
+             'element/quadrature.py:321-410).  A float32 LAPACK solve cannot be restated',
+             'bit for bit, so the values are a table: written by tests/golden/make_golden.py',
+             'from the reference\'s own output, one float32 per entry (hex literal).',
+             '"""', "", "POINTS = {"]
+    for fam in ("triangle", "tetra"):
+        for q in (1, 2, 3, 4):
+            p = np.asarray(arrays[f"facet_table/{fam}/q{q}/p"], dtype=np.float32)
+            F, Qf, D = p.shape
+            rows = []
+            for f in range(F):
+                pts = ", ".join("(" + ", ".join(f"float.fromhex('{float(v).hex()}')" for v in p[f, k]) + ",)"
+                                for k in range(Qf))
+                rows.append(f"        ({pts},),")
+            lines.append(f"    ({fam!r}, {q}): (")
+            lines += rows
+            lines.append("    ),")
+    lines.append("}")
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    print("wrote", path)
 
 
 if __name__ == "__main__":

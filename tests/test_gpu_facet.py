@@ -1,10 +1,11 @@
 """Parity of the CUDA facet (boundary) loads against the oracle and the
 reference's own FacetAssembler outputs (golden fixtures).
 
-Bars: float64 within 1e-12 relative (max-norm, relative to max|b|) of the
-oracle with the exact facet rule; within 1e-6 of the reference, whose facet
-rule is rounded to float32 (the oracle reproduces the reference to 1e-12
-when handed the reference's table, tests/test_oracle_golden.py); float32
+Bars: with the default facet rule (the reference's float32-built rule),
+float64 within 1e-12 relative (max-norm, relative to max|b|) of the
+reference's own outputs and of the oracle handed the reference's table;
+with ``facet_rule="exact"``, within 1e-12 of the oracle's exact float64 rule
+(and 1e-6 of the reference, whose rule is rounded to float32); float32
 within 1e-5; bitwise determinism run to run."""
 import math
 
@@ -18,6 +19,19 @@ from oracle import fem
 pytestmark = pytest.mark.gpu
 DEV = "cuda"
 MESHES = ["triangle", "triangle6", "tetra", "tetra10", "triangle6c", "tetra10c"]
+
+
+def ref_table(et, q):
+    """The reference's float32 facet table (weights, points) of the family of
+    ``et``, as stored in the facet fixture."""
+    g = np.load(fem_fixture())
+    fam = "triangle" if et.startswith("tri") else "tetra"
+    return g[f"facet_table/{fam}/q{q}/w"], g[f"facet_table/{fam}/q{q}/p"]
+
+
+def fem_fixture():
+    import os
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_facet.npz")
 
 
 def rel_err(a, b):
@@ -55,19 +69,23 @@ def mesh_of(g, et, dtype=torch.float64):
                                "is_top": torch.tensor(g[f"{et}/top"], device=DEV)})
 
 
-def run_case(mesh, case, q, gfield):
+def run_case(mesh, case, q, gfield, rule="reference"):
+    def make(cls, **kw):
+        asm = cls.from_mesh(mesh, quadrature_order=q, **kw)
+        asm.facet_rule = rule
+        return asm
     if case == "const":
-        return FacetOne.from_mesh(mesh, quadrature_order=q)(mesh.points)
+        return make(FacetOne)(mesh.points)
     if case == "vector":
-        return FacetVector.from_mesh(mesh, quadrature_order=q)(mesh.points)
+        return make(FacetVector)(mesh.points)
     if case == "func":
-        return FacetFunc.from_mesh(mesh, quadrature_order=q)(mesh.points)
+        return make(FacetFunc)(mesh.points)
     if case == "point":
-        return FacetPoint.from_mesh(mesh, quadrature_order=q)(mesh.points, point_data={"g": gfield})
-    return FacetOne.from_mesh(mesh, boundary_mask="is_top", quadrature_order=q)(mesh.points)
+        return make(FacetPoint)(mesh.points, point_data={"g": gfield})
+    return make(FacetOne, boundary_mask="is_top")(mesh.points)
 
 
-def oracle_case(g, et, case, q):
+def oracle_case(g, et, case, q, rule="reference"):
     pts, el = g[f"{et}/points"], g[f"{et}/elements"]
     dim = pts.shape[1]
     bd, top = g[f"{et}/boundary"], g[f"{et}/top"]
@@ -78,7 +96,8 @@ def oracle_case(g, et, case, q):
         "point": ("point", g[f"{et}/facet_g"], bd),
         "top": ("const", 1.0, top),
     }[case]
-    return fem.facet_load(pts, el, et.rstrip("c"), mask, q, kind, val)
+    tables = ref_table(et, q) if rule == "reference" else None
+    return fem.facet_load(pts, el, et.rstrip("c"), mask, q, kind, val, tables=tables)
 
 
 @pytest.mark.parametrize("et", MESHES)
@@ -88,11 +107,14 @@ def test_facet_loads_match_oracle_and_reference(golden_facet, et, q, case):
     g = golden_facet
     mesh = mesh_of(g, et)
     gfield = torch.tensor(g[f"{et}/facet_g"], device=DEV)
-    got = run_case(mesh, case, q, gfield).cpu().numpy()
     ref = g[f"{et}/facet_{case}/q{q}"]
+    got = run_case(mesh, case, q, gfield).cpu().numpy()           # default: the reference's rule
     assert got.shape == ref.shape
+    assert rel_err(got, ref) <= 1e-12
     assert rel_err(got, oracle_case(g, et, case, q)) <= 1e-12
-    assert rel_err(got, ref) <= 1e-6
+    exact = run_case(mesh, case, q, gfield, rule="exact").cpu().numpy()
+    assert rel_err(exact, oracle_case(g, et, case, q, rule="exact")) <= 1e-12
+    assert rel_err(exact, ref) <= 1e-6
 
 
 @pytest.mark.parametrize("et", MESHES)
@@ -122,7 +144,8 @@ def test_facet_loads_larger_curved_mesh(etype):
     mesh = tg.Mesh(points=pts.to(DEV), cells={etype: el.to(DEV)}, point_data={"is_boundary": bd.to(DEV)})
     for q in (2, 3):
         got = FacetPoint.from_mesh(mesh, quadrature_order=q)(mesh.points, point_data={"g": gf.to(DEV)})
-        ref = fem.facet_load(pts.numpy(), el.numpy(), etype, bd.numpy(), q, "point", gf.numpy())
+        ref = fem.facet_load(pts.numpy(), el.numpy(), etype, bd.numpy(), q, "point", gf.numpy(),
+                             tables=ref_table(etype, q))
         assert rel_err(got.cpu().numpy(), ref) <= 1e-12
 
 
@@ -190,7 +213,7 @@ def test_facet_load_gradient_wrt_point_data(golden_facet, et):
     b = FacetPoint.from_mesh(mesh, quadrature_order=3)(mesh.points, point_data={"g": field})
     w = rng.normal(size=b.shape[0])
     (b * torch.tensor(w, device=DEV)).sum().backward()
-    ref = fem.facet_load(pts, el, et.rstrip("c"), bd, 3, "point", w)
+    ref = fem.facet_load(pts, el, et.rstrip("c"), bd, 3, "point", w, tables=ref_table(et, 3))
     assert rel_err(field.grad.cpu().numpy(), ref) <= 1e-12
 
     t = [0.5, -1.0] if dim == 2 else [0.0, 0.3, -1.0]
@@ -202,8 +225,9 @@ def test_facet_load_gradient_wrt_point_data(golden_facet, et):
     field = g0.clone().requires_grad_(True)
     b = PointTraction.from_mesh(mesh, quadrature_order=2)(mesh.points, point_data={"p": field})
     assert rel_err(b.detach().cpu().numpy(),
-                   fem.facet_load(pts, el, et.rstrip("c"), bd, 2, "point", g0.cpu().numpy()[:, None] * np.array(t))) <= 1e-12
+                   fem.facet_load(pts, el, et.rstrip("c"), bd, 2, "point", g0.cpu().numpy()[:, None] * np.array(t),
+                                  tables=ref_table(et, 2))) <= 1e-12
     W = rng.normal(size=(pts.shape[0], dim))
     (b * torch.tensor(W.reshape(-1), device=DEV)).sum().backward()
-    ref = fem.facet_load(pts, el, et.rstrip("c"), bd, 2, "point", W @ np.array(t))
+    ref = fem.facet_load(pts, el, et.rstrip("c"), bd, 2, "point", W @ np.array(t), tables=ref_table(et, 2))
     assert rel_err(field.grad.cpu().numpy(), ref) <= 1e-12

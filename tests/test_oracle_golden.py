@@ -195,3 +195,22 @@ def test_oracle_clamped_elasticity_pipeline(golden_condense):
     assert rel_err(f_i, g["c2/f_i"]) <= 1e-12
     u = fem.recover(fem.spsolve(iptr, ic, iv, f_i), clamp)
     assert rel_err(u, g["c2/u"]) <= 1e-10
+
+
+@pytest.mark.parametrize("et", FACET_MESHES)
+@pytest.mark.parametrize("q", [1, 2, 3, 4])
+def test_package_reference_facet_rule_is_the_reference_table(golden_facet, et, q):
+    """The package's default facet rule carries the reference's float32 table
+    (weights and points bit for bit), and the oracle run on the package's
+    tables reproduces the reference's facet loads to rounding."""
+    from tensormesh_gb300.facet import facet_tables
+    g = golden_facet
+    etype = et.rstrip("c")
+    fam = "triangle" if etype.startswith("tri") else "tetra"
+    w, _, _, xi = facet_tables(etype, q, "reference")
+    assert np.array_equal(w, g[f"facet_table/{fam}/q{q}/w"])
+    assert np.array_equal(xi, g[f"facet_table/{fam}/q{q}/p"])
+    pts, el = g[f"{et}/points"], g[f"{et}/elements"]
+    for case, (kind, val, mask) in facet_cases(g, et).items():
+        got = fem.facet_load(pts, el, etype, mask, q, kind, val, tables=(w, xi))
+        assert rel_err(got, g[f"{et}/facet_{case}/q{q}"]) <= 1e-12, case
