@@ -333,11 +333,11 @@ extern "C" int64_t tm_patch_smem_bytes(int32_t element, int32_t form, int32_t n_
   bool load = form == TM_FORM_LOAD;
   size_t SE = load ? (size_t)B * H : (size_t)B * B * H * H;
   size_t HH = load ? H : (size_t)H * H;
-  size_t n = tmg::kMaxQuad + tmg::kMaxQuad * B + tmg::kMaxQuad * B * D + (size_t)plan->max_vtx * D;
+  size_t n = tmg::kMaxQuad + tmg::kMaxQuad * B + tmg::kMaxQuad * B * D;
   if (coef_kind == TM_COEF_POINT) n += (size_t)plan->max_vtx * (load ? H : 1);
   n += load ? (size_t)plan->max_rows * H : (size_t)plan->max_slots * HH;
   n += (size_t)chunk * SE;
-  return (int64_t)(n * es + (size_t)plan->max_rows * sizeof(int) + 16);
+  return (int64_t)(32 + (size_t)plan->max_vtx * D * 8 + n * es + (size_t)plan->max_rows * sizeof(int) + 16);
 }
 
 extern "C" int tm_batched_max_clusters(int32_t element, int32_t cluster, int64_t smem_bytes) {

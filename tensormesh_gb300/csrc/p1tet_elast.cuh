@@ -1,7 +1,9 @@
 // Specialised path for isotropic linear elasticity on P1 tetrahedra (FP64
 // emulated or FP32): same patch decomposition and fixed-order
 // row-owner accumulation as the generic kernel, with the element algebra in
-// closed form.
+// closed form on the patch frame's edge vectors (patch_frame.cuh).  A patch
+// with an ill-conditioned element or a modulus outside double-float's range
+// is redone in native FP64 by its CTA.
 //
 // With edge vectors d_k = X_{k+1} - X_0, the cross products C_1 = d_2 x d_3,
 // C_2 = d_3 x d_1, C_3 = d_1 x d_2, C_0 = -(C_1 + C_2 + C_3) and
@@ -25,9 +27,12 @@ constexpr int kElastStage = 24;  // staged values per element
 // index of the unordered pair (a, b) among the 10 dot products
 TM_D int pair4(int a, int b) { return tri4(a, b); }
 
-template <class T, class A, class RW>
-__global__ void __launch_bounds__(kThreads, 2)
-p1tet_elast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
+// One pass over the patch in arithmetic A; with kGuard (double-float) returns
+// false on every thread when the patch needs native FP64 (an ill-conditioned
+// element or a modulus outside double-float's range).
+template <class T, class A, class RW, bool kGuard>
+__device__ __forceinline__ bool p1tet_elast_pass(const tm_patch_plan& plan, const tm_assemble_args& args, int chunk,
+                                                 unsigned char* smem_raw) {
   using P = Ar<A>;
   using R = Rec<RW>;
   using S = typename P::S;
@@ -38,13 +43,13 @@ p1tet_elast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
   const int vbeg = plan.vptr[p], nv = plan.vptr[p + 1] - vbeg;
   const int ebeg = plan.eptr[p], ne = plan.eptr[p + 1] - ebeg;
   const int rbeg = plan.rptr[p], nr = plan.rptr[p + 1] - rbeg;
-  if (nr == 0) return;
+  if (nr == 0) return true;
 
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   int64_t* s_out0 = reinterpret_cast<int64_t*>(smem_raw);         // [kThreads/3] first dof value of each row
   uint32_t* s_rd = reinterpret_cast<uint32_t*>(s_out0 + kThreads); // [kThreads/3] acc slot | degree << 24
-  S* s_X = reinterpret_cast<S*>(s_rd + kThreads);                  // [max_vtx][3]
-  S* s_acc = s_X + plan.max_vtx * 3;                               // [max_slots][3][3]
+  unsigned long long* s_red = reinterpret_cast<unsigned long long*>(s_rd + kThreads);  // [3] (4 words reserved)
+  long long* s_R = reinterpret_cast<long long*>(s_red + 4);        // [max_vtx][3] integer frame
+  S* s_acc = reinterpret_cast<S*>(s_R + plan.max_vtx * 3);         // [max_slots][3][3]
   S* s_stage = s_acc + (int64_t)plan.max_slots * 9;                // [kElastStage][chunk]
 
   // ---- phase 0: row state; thread t owns component t % 3 of row t / 3
@@ -70,10 +75,9 @@ p1tet_elast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
       for (int j = 0; j < 3; ++j) s_acc[((ro + k) * 3 + comp) * 3 + j] = P::st(P::zero());
   }
   const T* pts = static_cast<const T*>(args.points);
-  for (int i = tid; i < nv * 3; i += kThreads) {
-    const int v = plan.vtx[vbeg + i / 3];
-    s_X[i] = P::st(P::in(pts[(int64_t)v * 3 + i % 3]));
-  }
+  const FrameInfo fr = patch_frame<3, T>(pts, plan.vtx + vbeg, nv, s_R, s_red);
+  if (fr.bad && kGuard) return false;  // a non-finite coordinate: the native pass writes nan
+  bool flag = kGuard && args.coef_kind == TM_COEF_SCALAR && !coef_in_range(args.scal[0]);
   const T* coef = static_cast<const T*>(args.coef);
   double wsum = 0.0;
   for (int q = 0; q < Q; ++q) wsum += args.tables[q];
@@ -103,17 +107,36 @@ p1tet_elast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
         if (per_elem) c_next = coef[plan.elem[pair + chunk]];
       }
       const int lv[4] = {(int)(cw.x & 0xffff), (int)(cw.x >> 16), (int)(cw.y & 0xffff), (int)(cw.y >> 16)};
-      A X[4][3];
-#pragma unroll
-      for (int b = 0; b < 4; ++b)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) X[b][d] = P::ld(s_X[lv[b] * 3 + d]);
       const A c = per_elem ? P::in(c_raw) : sc;
+      if (kGuard && per_elem && !coef_in_range((double)c_raw)) flag = true;
+      // edge vectors in frame units, exact to 2^-48 of themselves
       A dd[3][3];
+      if (fr.shortp) {
+        const int* r32 = reinterpret_cast<const int*>(s_R);
+        const ShortConv conv = short_conv(fr.t + fr.z - 62);
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
+        for (int d = 0; d < 3; ++d) {
+          const int r0 = r32[2 * (lv[0] * 3 + d)];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) dd[k][d] = P::sub(X[k + 1][d], X[0][d]);
+          for (int k = 0; k < 3; ++k) dd[k][d] = P::pair(conv(r32[2 * (lv[k + 1] * 3 + d)] - r0), 0.f);
+        }
+      } else if constexpr (std::is_same<A, double>::value) {
+        // native FP64 pass: the full 53 bits of every difference
+        const double esc = ldexp(1.0, fr.z - 62);
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) dd[k][d] = __ll2double_rn(s_R[lv[k + 1] * 3 + d] - s_R[lv[0] * 3 + d]) * esc;
+      } else {
+        float eh[3][3], el[3][3];
+        const int u = exact_edges<3, 3>(s_R, lv, eh, el);
+        if (u < 0 && kGuard) flag = true;
+        const float p2 = tm_pow2f(fr.z - (u < 0 ? 0 : u));
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) dd[k][d] = P::scale2(P::pair(eh[k][d], el[k][d]), p2);
+      }
       auto cross = [](const A* u, const A* v, A* out) {
         out[0] = P::sub(P::mul(u[1], v[2]), P::mul(u[2], v[1]));
         out[1] = P::sub(P::mul(u[2], v[0]), P::mul(u[0], v[2]));
@@ -126,6 +149,18 @@ p1tet_elast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
 #pragma unroll
       for (int d = 0; d < 3; ++d) C[0][d] = P::neg(P::add(P::add(C[1][d], C[2][d]), C[3][d]));
       const A det = P::add(P::add(P::mul(dd[0][0], C[1][0]), P::mul(dd[0][1], C[1][1])), P::mul(dd[0][2], C[1][2]));
+      if constexpr (kGuard) {
+        float trg = 0.f, tra = 0.f;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            trg = __fmaf_rn(P::hi(dd[k][d]), P::hi(dd[k][d]), trg);
+            tra = __fmaf_rn(P::hi(C[k + 1][d]), P::hi(C[k + 1][d]), tra);
+          }
+        const float dh = P::hi(det);
+        if (!(dh * dh >= 1e-30f && trg * tra <= kCondMax * (dh * dh))) flag = true;
+      }
       // 1/|det| = (1/sqrt(det^2))
       const A s = P::mul(P::mul(c, W), P::rsqrt(P::mul(det, det)));
       const int lo = le - cbeg;
@@ -143,7 +178,7 @@ p1tet_elast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
           s_stage[(14 + pair4(a, b)) * chunk + lo] = P::st(dot);
         }
     }
-    __syncthreads();
+    if (__syncthreads_or(kGuard && flag)) return false;
     // --- phase B: component `comp` of the row's blocks, incidence order -----
     if (owner) {
       for (;;) {
@@ -196,14 +231,27 @@ p1tet_elast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
     const int64_t o0 = s_out0[r] + (int64_t)i * 3 * deg;
     for (int k = lane; k < 3 * deg; k += 32) {
       const int kk = k / 3, j = k - 3 * (k / 3);
-      out[o0 + k] = (T)P::out(s_acc[((r0 + kk) * 3 + i) * 3 + j]);
+      out[o0 + k] = fr.bad ? T(NAN) : (T)tm_scale_pow2(P::out(s_acc[((r0 + kk) * 3 + i) * 3 + j]), fr.k);
     }
+  }
+  return true;
+}
+
+template <class T, class A, class RW>
+__global__ void __launch_bounds__(kThreads, 2)
+p1tet_elast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr bool kGuard = std::is_same<A, L2>::value;
+  if (p1tet_elast_pass<T, A, RW, kGuard>(plan, args, chunk, smem_raw)) return;
+  if constexpr (kGuard) {
+    __syncthreads();
+    p1tet_elast_pass<T, double, RW, false>(plan, args, chunk, smem_raw);
   }
 }
 
 inline size_t p1tet_elast_smem_bytes(const tm_patch_plan& plan, int chunk, size_t elem) {
-  const size_t n2 = (size_t)plan.max_vtx * 3 + (size_t)plan.max_slots * 9 + (size_t)kElastStage * chunk;
-  return (size_t)kThreads * (sizeof(int64_t) + sizeof(uint32_t)) + n2 * elem + 64;
+  const size_t n2 = (size_t)plan.max_slots * 9 + (size_t)kElastStage * chunk;
+  return (size_t)kThreads * (sizeof(int64_t) + sizeof(uint32_t)) + 32 + (size_t)plan.max_vtx * 3 * 8 + n2 * elem + 64;
 }
 
 // three threads per owned node row; node slots addressable in 24 bits

@@ -1,18 +1,38 @@
-// Specialised FP64 path for the headline case: P1 tetrahedra, Laplace form
-// with a per-element (or scalar / interpolated) coefficient, emulated FP64.
+// Specialised kernel of the headline case: P1 tetrahedra, Laplace form with a
+// scalar, per-element, nodal or per-quadrature-point coefficient, float64
+// (double-float arithmetic on the FP32 pipe) or float32.
 //
 // Same patch decomposition and deterministic row-owner accumulation as the
-// generic kernel (assemble_impl.cuh), with the arithmetic cut to what the
-// 1e-12 bar needs:
-//   * "lazy" double-float values (hi, lo) whose lo part is not renormalised
-//     after every operation (error-free products by FMA, TwoSum only where
-//     two leading parts are added);
-//   * 1/sqrt(det G) from the MUFU estimate plus one Newton step carried out
-//     in double-float, instead of IEEE division and square root;
-//   * the 10 unique entries of the symmetric element matrix are staged (not
-//     16).
+// generic kernel (assemble_impl.cuh); what is specific:
+//
+//  * the element algebra runs in the patch frame (patch_frame.cuh): the
+//    patch's vertices relative to its first vertex, scaled by a power of two,
+//    so the result does not depend on where the mesh sits or in which units;
+//  * the element matrix comes from the cross products of the edge vectors
+//    d_k = X_k - X_0: C_1 = d_2 x d_3, C_2 = d_3 x d_1, C_3 = d_1 x d_2 are
+//    det * grad N_1..3, so K_ab = c W C_a . C_b / |det| (a, b >= 1, W the sum
+//    of the quadrature weights, c the coefficient averaged over them) and row
+//    0 is minus the sum of the others.  Its rounding error grows like the
+//    element's aspect ratio (the metric-tensor form G = D^T D grows like its
+//    square);
+//  * "lazy" double-float values (hi, lo) whose lo part is not renormalised
+//    after every operation (error-free products by FMA, TwoSum only where two
+//    leading parts are added); 1 / |det| from the MUFU estimate plus one
+//    Newton step;
+//  * 10 unique values of the symmetric element matrix are staged; the stage is
+//    double-buffered so each chunk of elements costs one CTA barrier: the
+//    threads compute chunk c + 1 while the row owners consume chunk c.
+//
+// Two fallbacks keep the float64 result within the 1e-12 bar on every input:
+//  * an element whose conditioning proxy tr(G) tr(adj G) / det(G) exceeds
+//    kCondMax is computed in native FP64 by its thread (rare: slivers);
+//  * a patch with a coefficient or a value outside the range double-float can
+//    hold (or a non-finite coordinate) is redone by its CTA in native FP64 from
+//    the start (the decision is CTA-uniform: __syncthreads_or).
 #pragma once
 #include "assemble_impl.cuh"
+#include "patch_frame.cuh"
+#include <type_traits>
 
 namespace tmg {
 
@@ -29,6 +49,24 @@ TM_D L2 l2_rsqrt(L2 x) {
   const float r = __fadd_rn(__fsub_rn(1.0f, t.h), -t.l);  // 1 - x y0^2 (small)
   const float corr = __fmul_rn(__fmul_rn(0.5f, y0), r);
   return l2_norm(L2{y0, corr});
+}
+
+TM_D float tm_rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// 1/x for x > 0: MUFU estimate y0, then y0 + y0 r with the residual
+// r = 1 - x y0 formed from the error-free product x.h y0 = p + pe (1 - p is
+// exact: p lies within a few ulps of 1).
+TM_D L2 l2_rcp(L2 x) {
+  x = l2_norm(x);
+  const float y0 = tm_rcp_approx(x.h);
+  const float p = __fmul_rn(x.h, y0);
+  const float pe = __fmaf_rn(x.h, y0, -p);
+  const float r = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p), pe), __fmul_rn(x.l, y0));
+  return l2_norm(L2{y0, __fmul_rn(y0, r)});
 }
 
 // Unique-entry index of (a, b) in the staged upper triangle of a 4x4:
@@ -61,11 +99,13 @@ template <> struct Rec<uint32_t> {
 //   a=0: 0 1 2 3   a=1: 4 5 6 1   a=2: 7 8 2 5   a=3: 9 3 6 8
 constexpr uint64_t kTet4Stage = 0x8639528716543210ull;
 
-// Arithmetic policies: emulated FP64 (lazy double-float, stored as float2)
-// and plain FP32 (the float32 variant of the same kernel).
+// Arithmetic policies: emulated FP64 (lazy double-float, stored as float2),
+// native FP64 (the fallback) and plain FP32 (the float32 variant).
 template <class A> struct Ar;
 template <> struct Ar<L2> {
   using S = float2;
+  static TM_D L2 pair(float h, float l) { return L2{h, l}; }
+  static TM_D L2 scale2(L2 a, float p2) { return L2{__fmul_rn(a.h, p2), __fmul_rn(a.l, p2)}; }
   static TM_D L2 ld(S v) { return L2{v.x, v.y}; }
   static TM_D S st(L2 a) { return make_float2(a.h, a.l); }
   static TM_D L2 in(double x) { return l2_from(tm_from_double(x)); }
@@ -74,12 +114,36 @@ template <> struct Ar<L2> {
   static TM_D L2 sub(L2 a, L2 b) { return l2_sub(a, b); }
   static TM_D L2 mul(L2 a, L2 b) { return l2_mul(a, b); }
   static TM_D L2 neg(L2 a) { return l2_neg(a); }
+  static TM_D L2 abs(L2 a) { return a.h < 0.f ? l2_neg(a) : a; }
   static TM_D L2 rsqrt(L2 a) { return l2_rsqrt(a); }
+  static TM_D L2 rcp(L2 a) { return l2_rcp(a); }
   static TM_D L2 zero() { return L2{0.f, 0.f}; }
+  static TM_D float hi(L2 a) { return a.h; }
   static TM_D double out(S v) { return tm_to_double(df64{v.x, v.y}); }
+};
+template <> struct Ar<double> {
+  using S = double;
+  static TM_D double pair(float h, float l) { return (double)h + (double)l; }
+  static TM_D double scale2(double a, float p2) { return a * (double)p2; }
+  static TM_D double ld(S v) { return v; }
+  static TM_D S st(double a) { return a; }
+  static TM_D double in(double x) { return x; }
+  static TM_D double in(float x) { return (double)x; }
+  static TM_D double add(double a, double b) { return a + b; }
+  static TM_D double sub(double a, double b) { return a - b; }
+  static TM_D double mul(double a, double b) { return a * b; }
+  static TM_D double neg(double a) { return -a; }
+  static TM_D double abs(double a) { return fabs(a); }
+  static TM_D double rsqrt(double a) { return 1.0 / sqrt(a); }
+  static TM_D double rcp(double a) { return 1.0 / a; }
+  static TM_D double zero() { return 0.0; }
+  static TM_D float hi(double a) { return (float)a; }
+  static TM_D double out(S v) { return v; }
 };
 template <> struct Ar<float> {
   using S = float;
+  static TM_D float pair(float h, float l) { return __fadd_rn(h, l); }
+  static TM_D float scale2(float a, float p2) { return __fmul_rn(a, p2); }
   static TM_D float ld(S v) { return v; }
   static TM_D S st(float a) { return a; }
   static TM_D float in(double x) { return (float)x; }
@@ -88,190 +152,361 @@ template <> struct Ar<float> {
   static TM_D float sub(float a, float b) { return a - b; }
   static TM_D float mul(float a, float b) { return a * b; }
   static TM_D float neg(float a) { return -a; }
+  static TM_D float abs(float a) { return fabsf(a); }
   static TM_D float rsqrt(float a) { return rsqrtf(a); }
+  static TM_D float rcp(float a) { return 1.0f / a; }
   static TM_D float zero() { return 0.f; }
+  static TM_D float hi(float a) { return a; }
   static TM_D float out(S v) { return v; }
 };
 
-template <class T, class A, class RW>
-__global__ void __launch_bounds__(kThreads, 4)
-p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args, int chunk) {
+// Conditioning bound of the double-float element algebra: with frame
+// coordinates the cross-product form stays within a few 1e-13 of the element's
+// largest entry up to tr(G) tr(adj G) / det(G) = 1e4 (a regular tetrahedron
+// has 9, the six Kuhn tetrahedra of a cube 30, aspect ratio ~100 slivers
+// ~1e4); elements above it take the native FP64 path.
+constexpr float kCondMax = 1.0e4f;
+// A coefficient whose binary exponent lies outside +-kCoefExp would push the
+// frame element values out of float's exponent range (with room for the lo
+// parts); its patch is redone in native FP64.
+constexpr int kCoefExp = 60;
+
+TM_D bool coef_in_range(double c) {
+  const int e = (int)(((unsigned long long)__double_as_longlong(c) >> 52) & 0x7ff);
+  return c == 0.0 || (e >= 1023 - kCoefExp && e <= 1023 + kCoefExp);
+}
+
+// One element in native FP64 from the patch's integer frame (the cross-product
+// form; esc turns an integer difference into frame units); writes the 10
+// staged values as double-float.  Returns
+// false when a value does not fit double-float's range.
+__device__ __noinline__ bool p1tet_laplace_native_element(const long long* __restrict__ s_R, int l0, int l1, int l2,
+                                                          int l3, double esc, double cW, float2* stage, int stride) {
+  const int lv[4] = {l0, l1, l2, l3};
+  double dd[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) dd[k][d] = __ll2double_rn(s_R[lv[k + 1] * 3 + d] - s_R[lv[0] * 3 + d]) * esc;
+  double C[3][3];
+  auto cross = [](const double* u, const double* v, double* o) {
+    o[0] = u[1] * v[2] - u[2] * v[1];
+    o[1] = u[2] * v[0] - u[0] * v[2];
+    o[2] = u[0] * v[1] - u[1] * v[0];
+  };
+  cross(dd[1], dd[2], C[0]);
+  cross(dd[2], dd[0], C[1]);
+  cross(dd[0], dd[1], C[2]);
+  const double det = dd[0][0] * C[0][0] + dd[0][1] * C[0][1] + dd[0][2] * C[0][2];
+  const double s = cW / fabs(det);
+  double k[4][4];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = a; b < 3; ++b) k[a + 1][b + 1] = s * (C[a][0] * C[b][0] + C[a][1] * C[b][1] + C[a][2] * C[b][2]);
+  k[0][1] = -(k[1][1] + k[1][2] + k[1][3]);
+  k[0][2] = -(k[1][2] + k[2][2] + k[2][3]);
+  k[0][3] = -(k[1][3] + k[2][3] + k[3][3]);
+  k[0][0] = -(k[0][1] + k[0][2] + k[0][3]);
+  const double v[10] = {k[0][0], k[0][1], k[0][2], k[0][3], k[1][1], k[1][2], k[1][3], k[2][2], k[2][3], k[3][3]};
+  bool ok = true;
+#pragma unroll
+  for (int u = 0; u < 10; ++u) {
+    ok = ok && coef_in_range(v[u]);
+    const df64 t = tm_from_double(v[u]);
+    stage[u * stride] = make_float2(t.hi, t.lo);
+  }
+  return ok;
+}
+
+constexpr int kTetChunk = kThreads;  // elements staged per chunk (one per thread)
+
+// Shared-memory layout of one CTA.
+struct TetSmem {
+  unsigned long long* red;  // [3] (4 words reserved)
+  long long* R;             // [max_vtx * 3] integer frame coordinates
+  unsigned char* pc;        // [max_vtx] point coefficients (TM_COEF_POINT)
+  unsigned char* acc;       // [max_deg][nrp] row accumulators
+  unsigned char* stage;     // [2][10][kTetChunk]
+};
+
+// Row state of the thread that owns a row (owner == tid < nr).
+struct TetRow {
+  bool owner;
+  int deg, dpos, cur0, end;
+  int64_t o0;
+};
+
+// One pass over the patch in arithmetic A.  Returns false (on every thread)
+// when the patch must be redone in native FP64.
+template <class T, class A, class RW, bool kGuard>
+__device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, const tm_assemble_args& args,
+                                                   const TetSmem& sm, const TetRow& row, int nrp) {
   using P = Ar<A>;
+  using S = typename P::S;
   using R = Rec<RW>;
   const RW* recs = R::ptr(plan);
-  using S = typename P::S;
-  const int p = blockIdx.x;
-  const int tid = threadIdx.x;
+  const int p = blockIdx.x, tid = threadIdx.x;
   const int Q = args.n_quad;
   const int vbeg = plan.vptr[p], nv = plan.vptr[p + 1] - vbeg;
   const int ebeg = plan.eptr[p], ne = plan.eptr[p + 1] - ebeg;
-  const int rbeg = plan.rptr[p], nr = plan.rptr[p + 1] - rbeg;
-  if (nr == 0) return;
+  const long long* s_R = sm.R;
+  S* s_pc = reinterpret_cast<S*>(sm.pc);
+  S* s_acc = reinterpret_cast<S*>(sm.acc);
+  S* s_stage = reinterpret_cast<S*>(sm.stage);
 
-  // Accumulators are column-major over the patch's rows: entry k of local row
-  // lr sits at s_acc[k * nrp + lr], nrp = max_rows rounded up to 16, so the
-  // 16 lanes of a half-warp (consecutive rows) hit 16 distinct bank pairs
-  // whatever columns their incidences touch.
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int nrp = (plan.max_rows + 15) & ~15;
-  S* s_X = reinterpret_cast<S*>(smem_raw);                         // [max_vtx][3]
-  S* s_pc = s_X + plan.max_vtx * 3;                                // [max_vtx] point coef
-  const int pc_len = args.coef_kind == TM_COEF_POINT ? plan.max_vtx : 0;
-  S* s_acc = s_pc + pc_len;                                        // [max_deg][nrp]
-  S* s_stage = s_acc + plan.max_deg * nrp;                         // [10][chunk]
-
-  // ---- phase 0: row state (the launcher guarantees nr <= kThreads, so a
-  // thread owns at most one row; its incidence cursor and the next packed
-  // record stay in registers across chunks), coordinates, coefficients
-  const bool owner = tid < nr;
-  int cur = 0, end = 0, dpos = 0, deg = 0;
-  int64_t o0 = 0;
-  RW rec = R::kEnd;
-  S* acc = s_acc + tid;  // this thread's row: entry k at acc[k * nrp]
-  if (owner) {
-    const int r = plan.rows[rbeg + tid];
-    o0 = plan.indptr[r];
-    deg = (int)(plan.indptr[r + 1] - o0);
-    dpos = plan.rdiag[rbeg + tid];
-    cur = plan.iptr[rbeg + tid];
-    end = plan.iptr[rbeg + tid + 1];
-    if (cur < end) rec = recs[cur];
-    for (int k = 0; k < deg; ++k) acc[k * nrp] = P::st(P::zero());
-  }
+  // ---- phase 0: frame, point coefficients, zeroed accumulators, cursors
   const T* pts = static_cast<const T*>(args.points);
-  for (int i = tid; i < nv * 3; i += kThreads) {
-    const int v = plan.vtx[vbeg + i / 3];
-    s_X[i] = P::st(P::in(pts[(int64_t)v * 3 + i % 3]));
+  const FrameInfo fr = patch_frame<3, T>(pts, plan.vtx + vbeg, nv, sm.R, sm.red);
+  if (fr.bad) {
+    // a coordinate is inf or nan: the guarded pass hands the patch to the
+    // native pass, which writes nan to the patch's rows
+    if (kGuard) return false;
+    if (row.owner) {
+      T* out = static_cast<T*>(args.out);
+      for (int k = 0; k < row.deg; ++k) out[row.o0 + k] = T(NAN);
+    }
+    return true;
   }
+  const int kf = fr.k;
+  // integer difference -> frame units: 2^(t + z - 62) on short patches, 2^(z - 62) otherwise
+  const double esc = ldexp(1.0, (fr.shortp ? fr.t : 0) + fr.z - 62);
+  const ShortConv sconv = short_conv(fr.t + fr.z - 62);
   const T* coef = static_cast<const T*>(args.coef);
-  if (args.coef_kind == TM_COEF_POINT) {
+  if (args.coef_kind == TM_COEF_POINT)
     for (int i = tid; i < nv; i += kThreads) s_pc[i] = P::st(P::in(coef[plan.vtx[vbeg + i]]));
+  S* acc = s_acc + tid;  // this thread's row: entry k at acc[k * nrp]
+  int cur = 0;
+  RW rec = R::kEnd;
+  if (row.owner) {
+    for (int k = 0; k < row.deg; ++k) acc[k * nrp] = P::st(P::zero());
+    cur = row.cur0;
+    if (cur < row.end) rec = recs[cur];
   }
   double wsum = 0.0;
   for (int q = 0; q < Q; ++q) wsum += args.tables[q];
   const A W = P::in(wsum);
-  const A sc = P::in(args.scal[0]);
+  const double sc_raw = args.scal[0];
+  const A sc = P::in(sc_raw);
   const bool per_elem = args.coef_kind == TM_COEF_ELEMENT;
-  // element data of this thread's next element (threads tid < chunk handle
-  // element cbeg + tid of every chunk), loaded one chunk ahead
-  const bool worker = tid < chunk;
+  // element data of this thread's next element (thread tid handles element
+  // c * kTetChunk + tid of chunk c), loaded one chunk ahead
   uint2 cw_next = make_uint2(0u, 0u);
   T c_next = T(0);
-  if (worker && tid < ne) {
+  if (tid < ne) {
     cw_next = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)(ebeg + tid) * 4);
     if (per_elem) c_next = coef[plan.elem[ebeg + tid]];
   }
+  bool flag = kGuard && !coef_in_range((double)sc_raw) && args.coef_kind == TM_COEF_SCALAR;
   __syncthreads();
 
-  for (int cbeg = 0; cbeg < ne; cbeg += chunk) {
-    const int cend = min(ne, cbeg + chunk);
-    // --- phase A -------------------------------------------------------------
-    const int le = cbeg + tid;
-    if (worker && le < cend) {
-      const int pair = ebeg + le;
-      const uint2 cw = cw_next;
-      const T c_raw = c_next;
-      if (le + chunk < ne) {
-        cw_next = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)(pair + chunk) * 4);
-        if (per_elem) c_next = coef[plan.elem[pair + chunk]];
-      }
-      const int lv[4] = {(int)(cw.x & 0xffff), (int)(cw.x >> 16), (int)(cw.y & 0xffff), (int)(cw.y >> 16)};
-      A X[4][3];
+  // ---- phase A for chunk c: the element of thread tid into stage buffer c & 1
+  auto phase_a = [&](int ch) {
+    const int le = ch * kTetChunk + tid;
+    if (le >= ne) return;
+    const int pair = ebeg + le;
+    const uint2 cw = cw_next;
+    const T c_raw = c_next;
+    if (le + kTetChunk < ne) {
+      cw_next = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)(pair + kTetChunk) * 4);
+      if (per_elem) c_next = coef[plan.elem[pair + kTetChunk]];
+    }
+    const int lv[4] = {(int)(cw.x & 0xffff), (int)(cw.x >> 16), (int)(cw.y & 0xffff), (int)(cw.y >> 16)};
+    double c_dbl = 0.0;  // the coefficient in double where it is formed on the side
+    A c;
+    if (per_elem) {
+      c = P::in(c_raw);
+      c_dbl = (double)c_raw;
+    } else if (args.coef_kind == TM_COEF_POINT) {
+      // sum_q w_q sum_b N_b(q) c_b / W : the weighted vertex average
+      double cw_ = 0.0;
+      for (int q = 0; q < Q; ++q)
+        for (int b = 0; b < 4; ++b) cw_ += args.tables[q] * args.tables[Q + q * 4 + b] * (double)P::out(s_pc[lv[b]]);
+      c_dbl = cw_ / wsum;
+      c = P::in(c_dbl);
+    } else if (args.coef_kind == TM_COEF_QUAD) {
+      double cw_ = 0.0;
+      for (int q = 0; q < Q; ++q) cw_ += args.tables[q] * (double)coef[(int64_t)plan.elem[pair] * Q + q];
+      c_dbl = cw_ / wsum;
+      c = P::in(c_dbl);
+    } else {
+      c = sc;
+      c_dbl = sc_raw;
+    }
+    if (kGuard && !coef_in_range(c_dbl)) flag = true;
+    // edge vectors, exact to 2^-48 of themselves, equal to 2^e_sh times their frame values
+    A d[3][3];
+    int e_sh;
+    if (fr.shortp) {
+      // short patch: |difference| < 2^22, converted exactly into frame units
+      const int* r32 = reinterpret_cast<const int*>(s_R);
 #pragma unroll
-      for (int b = 0; b < 4; ++b)
+      for (int j = 0; j < 3; ++j) {
+        const int r0 = r32[2 * (lv[0] * 3 + j)];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) X[b][d] = P::ld(s_X[lv[b] * 3 + d]);
-      A c;
-      if (per_elem) {
-        c = P::in(c_raw);
-      } else if (args.coef_kind == TM_COEF_POINT) {
-        // sum_q w_q sum_b N_b(q) c_b / W : P1 -> weighted vertex average
-        double cw_ = 0.0;
-        for (int q = 0; q < Q; ++q)
-          for (int b = 0; b < 4; ++b) cw_ += args.tables[q] * args.tables[Q + q * 4 + b] * P::out(s_pc[lv[b]]);
-        c = P::in(cw_ / wsum);
-      } else if (args.coef_kind == TM_COEF_QUAD) {
-        double cw_ = 0.0;
-        for (int q = 0; q < Q; ++q) cw_ += args.tables[q] * (double)coef[(int64_t)plan.elem[pair] * Q + q];
-        c = P::in(cw_ / wsum);
-      } else {
-        c = sc;
+        for (int k = 0; k < 3; ++k) d[k][j] = P::pair(sconv(r32[2 * (lv[k + 1] * 3 + j)] - r0), 0.f);
       }
-      A d[3][3];
+      e_sh = 0;
+    } else {
+      float eh[3][3], el[3][3];
+      const int u = exact_edges<3, 3>(s_R, lv, eh, el);
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int dd = 0; dd < 3; ++dd) d[k][dd] = P::sub(X[k + 1][dd], X[0][dd]);
-      auto dot3 = [](const A* a, const A* b) {
-        return P::add(P::add(P::mul(a[0], b[0]), P::mul(a[1], b[1])), P::mul(a[2], b[2]));
-      };
-      auto cof = [](A a, A b, A c_, A d_) { return P::sub(P::mul(a, b), P::mul(c_, d_)); };
-      const A G00 = dot3(d[0], d[0]), G11 = dot3(d[1], d[1]), G22 = dot3(d[2], d[2]);
-      const A G01 = dot3(d[0], d[1]), G02 = dot3(d[0], d[2]), G12 = dot3(d[1], d[2]);
-      const A A00 = cof(G11, G22, G12, G12), A11 = cof(G00, G22, G02, G02), A22 = cof(G00, G11, G01, G01);
-      const A A01 = cof(G02, G12, G01, G22), A02 = cof(G01, G12, G02, G11), A12 = cof(G01, G02, G00, G12);
-      const A detG = P::add(P::add(P::mul(G00, A00), P::mul(G01, A01)), P::mul(G02, A02));
-      const A s = P::mul(P::mul(c, W), P::rsqrt(detG));
-      const A k11 = P::mul(s, A00), k22 = P::mul(s, A11), k33 = P::mul(s, A22);
-      const A k12 = P::mul(s, A01), k13 = P::mul(s, A02), k23 = P::mul(s, A12);
-      const A k01 = P::neg(P::add(P::add(k11, k12), k13));
-      const A k02 = P::neg(P::add(P::add(k12, k22), k23));
-      const A k03 = P::neg(P::add(P::add(k13, k23), k33));
-      const A k00 = P::neg(P::add(P::add(k01, k02), k03));
-      const int lo = le - cbeg;
-      const A vals[10] = {k00, k01, k02, k03, k11, k12, k13, k22, k23, k33};
-#pragma unroll
-      for (int u = 0; u < 10; ++u) s_stage[u * chunk + lo] = P::st(vals[u]);
+        for (int j = 0; j < 3; ++j) d[k][j] = P::pair(eh[k][j], el[k][j]);
+      e_sh = u - fr.z;   // u < 0 (a degenerate element) fails the conditioning test below
     }
-    __syncthreads();
-    // --- phase B: the row owner adds its incidences of this chunk (fixed
-    // order).  The diagonal is summed in registers and added once per chunk;
-    // the three off-diagonal contributions of an incidence hit distinct
-    // columns, so their read-modify-writes are issued together.  The record
-    // that ends the loop is the first one of the next chunk.
-    if (owner) {
-      A dg = P::zero();
-      bool any = false;
-      for (;;) {
-        const int lel = R::elem(rec);
-        if (lel >= cend) break;  // also the end record (its element field is past every chunk)
-        const RW next = (cur + 1 < end) ? recs[cur + 1] : R::kEnd;
-        const int a = R::a(rec);
-        const int lo = lel - cbeg;
-        const uint32_t u = (uint32_t)(kTet4Stage >> (16 * a));
-        dg = P::add(dg, P::ld(s_stage[(int)(u & 15u) * chunk + lo]));
-        int pos[3];
-        S v[3], old[3];
+    auto cross = [](const A* u, const A* v, A* o) {
+      o[0] = P::sub(P::mul(u[1], v[2]), P::mul(u[2], v[1]));
+      o[1] = P::sub(P::mul(u[2], v[0]), P::mul(u[0], v[2]));
+      o[2] = P::sub(P::mul(u[0], v[1]), P::mul(u[1], v[0]));
+    };
+    auto dot3 = [](const A* u, const A* v) {
+      return P::add(P::add(P::mul(u[0], v[0]), P::mul(u[1], v[1])), P::mul(u[2], v[2]));
+    };
+    A C[3][3];
+    cross(d[1], d[2], C[0]);
+    cross(d[2], d[0], C[1]);
+    cross(d[0], d[1], C[2]);
+    const A det = dot3(d[0], C[0]);
+    const A D11 = dot3(C[0], C[0]), D22 = dot3(C[1], C[1]), D33 = dot3(C[2], C[2]);
+    S* st = s_stage + (ch & 1) * 10 * kTetChunk + tid;
+    if constexpr (kGuard) {
+      float trg = 0.f;
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          pos[j] = R::pos(rec, j) * nrp;
-          v[j] = s_stage[(int)((u >> (4 * j + 4)) & 15u) * chunk + lo];
-        }
+      for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) old[j] = acc[pos[j]];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) acc[pos[j]] = P::st(P::add(P::ld(old[j]), P::ld(v[j])));
-        any = true;
-        rec = next;
-        ++cur;
+        for (int j = 0; j < 3; ++j) trg = __fmaf_rn(P::hi(d[k][j]), P::hi(d[k][j]), trg);
+      const float dh = P::hi(det);
+      const float tra = P::hi(D11) + P::hi(D22) + P::hi(D33);
+      if (!(e_sh >= -100 && e_sh <= 100 && dh * dh >= 1e-30f && trg * tra <= kCondMax * (dh * dh))) {
+        // ill-conditioned, degenerate, or tiny against its patch (frame
+        // products near float's underflow): native FP64 on this thread
+        if (!p1tet_laplace_native_element(s_R, lv[0], lv[1], lv[2], lv[3], esc, c_dbl * wsum,
+                                          reinterpret_cast<float2*>(st), kTetChunk))
+          flag = true;
+        return;
       }
-      if (any) acc[dpos * nrp] = P::st(P::add(P::ld(acc[dpos * nrp]), dg));
     }
-    __syncthreads();
+    // the edges are 2^e_sh times their frame values and K scales as length^1
+    const A s = P::scale2(P::mul(P::mul(c, W), P::rcp(P::abs(det))), tm_pow2f(-e_sh));
+    const A k11 = P::mul(s, D11), k22 = P::mul(s, D22), k33 = P::mul(s, D33);
+    const A k12 = P::mul(s, dot3(C[0], C[1])), k13 = P::mul(s, dot3(C[0], C[2])), k23 = P::mul(s, dot3(C[1], C[2]));
+    const A k01 = P::neg(P::add(P::add(k11, k12), k13));
+    const A k02 = P::neg(P::add(P::add(k12, k22), k23));
+    const A k03 = P::neg(P::add(P::add(k13, k23), k33));
+    const A k00 = P::neg(P::add(P::add(k01, k02), k03));
+    const A vals[10] = {k00, k01, k02, k03, k11, k12, k13, k22, k23, k33};
+#pragma unroll
+    for (int u = 0; u < 10; ++u) st[u * kTetChunk] = P::st(vals[u]);
+  };
+
+  // ---- phase B for chunk c: the row owner adds its incidences of the chunk
+  // (fixed order).  The diagonal is summed in registers and added once per
+  // chunk; the three off-diagonal contributions of an incidence hit distinct
+  // columns, so their read-modify-writes are issued together.  The record that
+  // ends the loop is the first one of the next chunk.
+  auto phase_b = [&](int ch) {
+    if (!row.owner) return;
+    const int cbeg = ch * kTetChunk, cend = cbeg + kTetChunk;
+    const S* stg = s_stage + (ch & 1) * 10 * kTetChunk;
+    A dg = P::zero();
+    bool any = false;
+    for (;;) {
+      const int lel = R::elem(rec);
+      if (lel >= cend) break;  // also the end record (its element field is past every chunk)
+      const RW next = (cur + 1 < row.end) ? recs[cur + 1] : R::kEnd;
+      const int a = R::a(rec);
+      const int lo = lel - cbeg;
+      const uint32_t u = (uint32_t)(kTet4Stage >> (16 * a));
+      dg = P::add(dg, P::ld(stg[(int)(u & 15u) * kTetChunk + lo]));
+      int pos[3];
+      S v[3], old[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        pos[j] = R::pos(rec, j) * nrp;
+        v[j] = stg[(int)((u >> (4 * j + 4)) & 15u) * kTetChunk + lo];
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) old[j] = acc[pos[j]];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) acc[pos[j]] = P::st(P::add(P::ld(old[j]), P::ld(v[j])));
+      any = true;
+      rec = next;
+      ++cur;
+    }
+    if (any) acc[row.dpos * nrp] = P::st(P::add(P::ld(acc[row.dpos * nrp]), dg));
+  };
+
+  const int nch = (ne + kTetChunk - 1) / kTetChunk;
+  if (nch > 0) phase_a(0);
+  for (int c = 0; c < nch; ++c) {
+    // stage c is complete and stage c + 1 is free (its last reader was phase B
+    // of chunk c - 1)
+    if (__syncthreads_or(kGuard && flag)) return false;
+    if (c + 1 < nch) phase_a(c + 1);
+    phase_b(c);
   }
-  // --- write the finished row: only its owner ever touched it, so no barrier
-  // is needed; consecutive lanes write consecutive rows' k-th entries
-  if (owner) {
+  // ---- write the finished row: only its owner ever touched it, so no
+  // barrier is needed; consecutive lanes write consecutive rows' k-th entries
+  if (row.owner) {
     T* out = static_cast<T*>(args.out);
-    for (int k = 0; k < deg; ++k) out[o0 + k] = (T)P::out(acc[k * nrp]);
+    for (int k = 0; k < row.deg; ++k) out[row.o0 + k] = (T)tm_scale_pow2(P::out(acc[k * nrp]), kf);
+  }
+  return true;
+}
+
+template <class T, class A, class RW>
+__global__ void __launch_bounds__(kThreads, 3)
+p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args) {
+  constexpr bool kGuard = std::is_same<A, L2>::value;
+  using S = typename Ar<A>::S;
+  const int p = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int rbeg = plan.rptr[p], nr = plan.rptr[p + 1] - rbeg;
+  if (nr == 0) return;
+
+  // Accumulators are column-major over the patch's rows: entry k of local row
+  // lr sits at acc[k * nrp + lr], nrp = max_rows rounded up to 16, so the
+  // 16 lanes of a half-warp (consecutive rows) hit 16 distinct bank pairs
+  // whatever columns their incidences touch.
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nrp = (plan.max_rows + 15) & ~15;
+  TetSmem sm;
+  sm.red = reinterpret_cast<unsigned long long*>(smem_raw);
+  sm.R = reinterpret_cast<long long*>(smem_raw + 32);
+  unsigned char* q = smem_raw + 32 + (size_t)plan.max_vtx * 3 * 8;
+  sm.pc = q;
+  if (args.coef_kind == TM_COEF_POINT) q += ((size_t)plan.max_vtx * 8 + 15) & ~size_t(15);
+  sm.acc = q;
+  q += (size_t)plan.max_deg * nrp * sizeof(S);
+  sm.stage = q;
+
+  TetRow row;
+  row.owner = tid < nr;
+  row.deg = row.dpos = row.cur0 = row.end = 0;
+  row.o0 = 0;
+  if (row.owner) {
+    const int r = plan.rows[rbeg + tid];
+    row.o0 = plan.indptr[r];
+    row.deg = (int)(plan.indptr[r + 1] - row.o0);
+    row.dpos = plan.rdiag[rbeg + tid];
+    row.cur0 = plan.iptr[rbeg + tid];
+    row.end = plan.iptr[rbeg + tid + 1];
+  }
+  if (p1tet_laplace_pass<T, A, RW, kGuard>(plan, args, sm, row, nrp)) return;
+  if constexpr (kGuard) {
+    __syncthreads();  // every thread is done with the double-float pass's shared memory
+    p1tet_laplace_pass<T, double, RW, false>(plan, args, sm, row, nrp);
   }
 }
 
-inline size_t p1tet_smem_bytes(const tm_patch_plan& plan, int coef_kind, int chunk, size_t elem = sizeof(float2)) {
+inline size_t p1tet_smem_bytes(const tm_patch_plan& plan, int coef_kind, size_t elem) {
   const size_t nrp = (size_t)((plan.max_rows + 15) & ~15);
-  size_t n2 = (size_t)plan.max_vtx * 3 + (coef_kind == TM_COEF_POINT ? plan.max_vtx : 0) +
-              (size_t)plan.max_deg * nrp + (size_t)10 * chunk;
-  return n2 * elem + 64;
+  size_t b = 32 + (size_t)plan.max_vtx * 3 * 8;
+  if (coef_kind == TM_COEF_POINT) b += ((size_t)plan.max_vtx * 8 + 15) & ~size_t(15);
+  b += (size_t)plan.max_deg * nrp * elem + (size_t)2 * 10 * kTetChunk * elem;
+  return b;
 }
 
 // The fast path needs every patch to own at most kThreads rows (one row per
@@ -285,18 +520,12 @@ inline int launch_p1tet_kernel(const tm_patch_plan& plan, const tm_assemble_args
   int dev = 0, max_optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  int chunk = kThreads;
-  const size_t es = sizeof(typename Ar<A>::S);
-  size_t bytes = p1tet_smem_bytes(plan, args.coef_kind, chunk, es);
-  while (bytes > (size_t)max_optin && chunk > 32) {
-    chunk /= 2;
-    bytes = p1tet_smem_bytes(plan, args.coef_kind, chunk, es);
-  }
+  const size_t bytes = p1tet_smem_bytes(plan, args.coef_kind, sizeof(typename Ar<A>::S));
   if (bytes > (size_t)max_optin) return TM_ERR_INDEX;
   auto kern = p1tet_laplace_fast_kernel<T, A, RW>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
     return TM_ERR_CUDA;
-  kern<<<plan.n_patches, kThreads, bytes, stream>>>(plan, args, chunk);
+  kern<<<plan.n_patches, kThreads, bytes, stream>>>(plan, args);
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
 
