@@ -341,6 +341,38 @@ int tm_pcg_jacobi_noalloc(int64_t n, const int64_t* indptr, const int32_t* indic
                           const float* b, float* x, double rtol, double atol, int32_t maxiter, int32_t* out_iters,
                           double* out_res, void* stream);
 
+/*
+ * CSR pattern of a mesh on the GPU (replaces the reference's from_mesh pattern
+ * build, assemble/element_assembler.py:838-866, and its per-entry slot map
+ * `elem_eids`).  elements: [n_elements][n_basis] int32 node ids in
+ * [0, n_points) (device).  Two calls:
+ *   tm_pattern_count writes indptr [n_points + 1] (int64): the row offsets of
+ *     the unique (row, col) pairs of every element's node pairs;
+ *   tm_pattern_fill (after the caller has read nnz = indptr[n_points] and
+ *     allocated) writes indices [nnz] (int32, ascending inside each row) and,
+ *     when out_slots is not NULL, slots [n_elements][n_basis][n_basis]
+ *     (int64): the CSR position of entry (row = el[e][a], col = el[e][b]).
+ * `work` (device, tm_pattern_workspace_bytes) carries the node -> element
+ * incidence from the first call to the second.  Deterministic; no host
+ * synchronisation inside.
+ */
+int64_t tm_pattern_workspace_bytes(int64_t n_elements, int32_t n_basis, int64_t n_points);
+int tm_pattern_count(const int32_t* elements, int64_t n_elements, int32_t n_basis, int64_t n_points, void* work,
+                     int64_t* out_indptr, void* stream);
+int tm_pattern_fill(const int32_t* elements, int64_t n_elements, int32_t n_basis, int64_t n_points, const void* work,
+                    const int64_t* indptr, int32_t* out_indices, int64_t* out_slots, void* stream);
+
+/*
+ * Self-test of the bounded grid barrier the PCG kernels use (no counterpart
+ * in the reference: the reference has no device-side waits).  Launches
+ * n_blocks cooperative CTAs of which one never arrives at the barrier; the
+ * others give up after `spins` polls 32 ns apart (at most the PCG kernels'
+ * ~1 s limit) and record TM_ERR_TIMEOUT, which is returned in *out_status.
+ * `work` is device memory of at least 64 bytes.  Synchronises `stream`.
+ * Returns TM_OK when the test ran.
+ */
+int tm_selftest_barrier_timeout(int32_t n_blocks, int64_t spins, int32_t* out_status, void* work, void* stream);
+
 /* 1/diag(A) with missing diagonals taken as 1 (torch_solve.py:24-59). */
 int tm_csr_diagonal_inverse(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
                             const void* values, void* out, void* stream);

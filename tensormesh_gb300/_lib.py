@@ -37,6 +37,7 @@ EXPORTS = [
     "tm_mpnn_input_fwd", "tm_mpnn_layer_fwd", "tm_mpnn_readout_fwd", "tm_mpnn_readout_bwd",
     "tm_mpnn_layer_bwd", "tm_mpnn_input_bwd", "tm_gather_axpy_f32",
     "tm_pcg_jacobi_noalloc", "tm_twolevel_apply", "tm_neohookean", "tm_facet_load",
+    "tm_selftest_barrier_timeout", "tm_pattern_workspace_bytes", "tm_pattern_count", "tm_pattern_fill",
 ]
 
 P = ctypes.c_void_p
@@ -135,7 +136,12 @@ def _declare(lib):
         "tm_twolevel_apply": [ctypes.POINTER(TwoLevel), P, P, P],
         "tm_neohookean": [i32, i32, i32, P, P, P, i64, P, ctypes.c_double, ctypes.c_double, P, P, P],
         "tm_facet_load": [i32, i32, i32, P, P, P, P, i64, i32, P, ctypes.POINTER(ctypes.c_double), i32, P, P, P],
+        "tm_selftest_barrier_timeout": [i32, i64, ctypes.POINTER(i32), P, P],
+        "tm_pattern_count": [P, i64, i32, i64, P, P, P],
+        "tm_pattern_fill": [P, i64, i32, i64, P, P, P, P, P],
     }
+    lib.tm_pattern_workspace_bytes.argtypes = [i64, i32, i64]
+    lib.tm_pattern_workspace_bytes.restype = i64
     lib.tm_patch_smem_bytes.argtypes = [i32, i32, i32, i32, ctypes.POINTER(PatchPlan), i32, i32]
     lib.tm_patch_smem_bytes.restype = i64
     lib.tm_pcg_workspace_bytes.argtypes = [i32, i64, i64, i32]

@@ -53,7 +53,10 @@ class MeshTopology:
         self._elements_long = elements.long()
         self.n_points = int(points.shape[0])
         self.n_elements = int(elements.shape[0])
+        self.timings = {}  # seconds of the pattern build and of each patch plan (device work included)
+        t0 = _now(elements.device)
         self.pattern = node_pattern(elements, self.n_points)
+        self.timings["pattern_s"] = _now(elements.device) - t0
         self._coords = points.detach()
         self._plans = {}
         self.plan, self._plan_struct = self.plan_for(1)
@@ -70,8 +73,10 @@ class MeshTopology:
         if budget is None:
             budget = self._SLOT_BUDGET.get(H, max(64, 6144 // (H * H)))
         if budget not in self._plans:
+            t0 = _now(self._coords.device)
             plan = PatchPlan(self._elements_long, self._coords, self.pattern, slot_budget=budget)
             self._plans[budget] = (plan, plan.to_struct())
+            self.timings[f"plan_{budget}_s"] = _now(self._coords.device) - t0
         return self._plans[budget]
 
     def dof_pattern(self, H: int):
@@ -82,6 +87,14 @@ class MeshTopology:
     @property
     def plan_struct(self):
         return self._plan_struct
+
+
+def _now(device) -> float:
+    """Host time after the device has finished its queued work."""
+    import time
+    if torch.device(device).type == "cuda":
+        torch.cuda.synchronize(device)
+    return time.perf_counter()
 
 
 _TOPO_CACHE: Dict[tuple, MeshTopology] = {}

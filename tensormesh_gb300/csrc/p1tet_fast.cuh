@@ -19,16 +19,16 @@
 //    after every operation (error-free products by FMA, TwoSum only where two
 //    leading parts are added); 1 / |det| from the MUFU estimate plus one
 //    Newton step;
-//  * 10 unique values of the symmetric element matrix are staged; the stage is
-//    double-buffered so each chunk of elements costs one CTA barrier: the
-//    threads compute chunk c + 1 while the row owners consume chunk c.
+//  * 10 unique values of the symmetric element matrix are staged (one stage
+//    of 256 elements: measured on GB300, a double-buffered stage with one
+//    barrier per chunk costs more through the lost occupancy than it saves);
+//  * 64 registers, so four CTAs share an SM.
 //
-// Two fallbacks keep the float64 result within the 1e-12 bar on every input:
-//  * an element whose conditioning proxy tr(G) tr(adj G) / det(G) exceeds
-//    kCondMax is computed in native FP64 by its thread (rare: slivers);
-//  * a patch with a coefficient or a value outside the range double-float can
-//    hold (or a non-finite coordinate) is redone by its CTA in native FP64 from
-//    the start (the decision is CTA-uniform: __syncthreads_or).
+// The float64 result stays within the 1e-12 bar on every input: a patch with
+// an element whose conditioning proxy tr(G) tr(adj G) / det(G) exceeds
+// kCondMax (slivers), a coefficient outside the range double-float can hold,
+// or a non-finite coordinate, is redone by its CTA in native FP64 from the
+// start (the decision is CTA-uniform: __syncthreads_or).
 #pragma once
 #include "assemble_impl.cuh"
 #include "patch_frame.cuh"
@@ -176,50 +176,20 @@ TM_D bool coef_in_range(double c) {
   return c == 0.0 || (e >= 1023 - kCoefExp && e <= 1023 + kCoefExp);
 }
 
-// One element in native FP64 from the patch's integer frame (the cross-product
-// form; esc turns an integer difference into frame units); writes the 10
-// staged values as double-float.  Returns
-// false when a value does not fit double-float's range.
-__device__ __noinline__ bool p1tet_laplace_native_element(const long long* __restrict__ s_R, int l0, int l1, int l2,
-                                                          int l3, double esc, double cW, float2* stage, int stride) {
-  const int lv[4] = {l0, l1, l2, l3};
-  double dd[3][3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
-#pragma unroll
-    for (int d = 0; d < 3; ++d) dd[k][d] = __ll2double_rn(s_R[lv[k + 1] * 3 + d] - s_R[lv[0] * 3 + d]) * esc;
-  double C[3][3];
-  auto cross = [](const double* u, const double* v, double* o) {
-    o[0] = u[1] * v[2] - u[2] * v[1];
-    o[1] = u[2] * v[0] - u[0] * v[2];
-    o[2] = u[0] * v[1] - u[1] * v[0];
-  };
-  cross(dd[1], dd[2], C[0]);
-  cross(dd[2], dd[0], C[1]);
-  cross(dd[0], dd[1], C[2]);
-  const double det = dd[0][0] * C[0][0] + dd[0][1] * C[0][1] + dd[0][2] * C[0][2];
-  const double s = cW / fabs(det);
-  double k[4][4];
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int b = a; b < 3; ++b) k[a + 1][b + 1] = s * (C[a][0] * C[b][0] + C[a][1] * C[b][1] + C[a][2] * C[b][2]);
-  k[0][1] = -(k[1][1] + k[1][2] + k[1][3]);
-  k[0][2] = -(k[1][2] + k[2][2] + k[2][3]);
-  k[0][3] = -(k[1][3] + k[2][3] + k[3][3]);
-  k[0][0] = -(k[0][1] + k[0][2] + k[0][3]);
-  const double v[10] = {k[0][0], k[0][1], k[0][2], k[0][3], k[1][1], k[1][2], k[1][3], k[2][2], k[2][3], k[3][3]};
-  bool ok = true;
-#pragma unroll
-  for (int u = 0; u < 10; ++u) {
-    ok = ok && coef_in_range(v[u]);
-    const df64 t = tm_from_double(v[u]);
-    stage[u * stride] = make_float2(t.hi, t.lo);
-  }
-  return ok;
-}
-
 constexpr int kTetChunk = kThreads;  // elements staged per chunk (one per thread)
+
+// A double in double-float for 2^-74 <= |x| < 2^128: hi = x truncated to 24
+// significant bits, lo = the low 29 bits rounded to float (2^-48 of x).  The
+// fast pass uses it for coefficients it has checked with coef_in_range (any
+// other value sends the patch to the native pass, so its result is unused).
+TM_D L2 l2_from_double_in_range(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hw = (unsigned)(b >> 32);
+  const unsigned e = (hw >> 20) & 0x7ffu;
+  const float h = __uint_as_float((hw & 0x80000000u) | ((e - 896u) << 23) | ((unsigned)(b >> 29) & 0x7fffffu));
+  const float l = __fmul_rn(__int2float_rn((int)(b & 0x1fffffffull)), __uint_as_float((e - 948u) << 23));
+  return L2{h, (hw & 0x80000000u) ? -l : l};
+}
 
 // Shared-memory layout of one CTA.
 struct TetSmem {
@@ -227,7 +197,7 @@ struct TetSmem {
   long long* R;             // [max_vtx * 3] integer frame coordinates
   unsigned char* pc;        // [max_vtx] point coefficients (TM_COEF_POINT)
   unsigned char* acc;       // [max_deg][nrp] row accumulators
-  unsigned char* stage;     // [2][10][kTetChunk]
+  unsigned char* stage;     // [10][kTetChunk]
 };
 
 // Row state of the thread that owns a row (owner == tid < nr).
@@ -269,8 +239,6 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
     return true;
   }
   const int kf = fr.k;
-  // integer difference -> frame units: 2^(t + z - 62) on short patches, 2^(z - 62) otherwise
-  const double esc = ldexp(1.0, (fr.shortp ? fr.t : 0) + fr.z - 62);
   const ShortConv sconv = short_conv(fr.t + fr.z - 62);
   const T* coef = static_cast<const T*>(args.coef);
   if (args.coef_kind == TM_COEF_POINT)
@@ -315,7 +283,8 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
     double c_dbl = 0.0;  // the coefficient in double where it is formed on the side
     A c;
     if (per_elem) {
-      c = P::in(c_raw);
+      if constexpr (std::is_same<A, L2>::value) c = l2_from_double_in_range((double)c_raw);
+      else c = P::in(c_raw);
       c_dbl = (double)c_raw;
     } else if (args.coef_kind == TM_COEF_POINT) {
       // sum_q w_q sum_b N_b(q) c_b / W : the weighted vertex average
@@ -370,7 +339,7 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
     cross(d[0], d[1], C[2]);
     const A det = dot3(d[0], C[0]);
     const A D11 = dot3(C[0], C[0]), D22 = dot3(C[1], C[1]), D33 = dot3(C[2], C[2]);
-    S* st = s_stage + (ch & 1) * 10 * kTetChunk + tid;
+    S* st = s_stage + tid;
     if constexpr (kGuard) {
       float trg = 0.f;
 #pragma unroll
@@ -381,10 +350,8 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
       const float tra = P::hi(D11) + P::hi(D22) + P::hi(D33);
       if (!(e_sh >= -100 && e_sh <= 100 && dh * dh >= 1e-30f && trg * tra <= kCondMax * (dh * dh))) {
         // ill-conditioned, degenerate, or tiny against its patch (frame
-        // products near float's underflow): native FP64 on this thread
-        if (!p1tet_laplace_native_element(s_R, lv[0], lv[1], lv[2], lv[3], esc, c_dbl * wsum,
-                                          reinterpret_cast<float2*>(st), kTetChunk))
-          flag = true;
+        // products near float's underflow): the patch goes native
+        flag = true;
         return;
       }
     }
@@ -409,7 +376,7 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
   auto phase_b = [&](int ch) {
     if (!row.owner) return;
     const int cbeg = ch * kTetChunk, cend = cbeg + kTetChunk;
-    const S* stg = s_stage + (ch & 1) * 10 * kTetChunk;
+    const S* stg = s_stage;
     A dg = P::zero();
     bool any = false;
     for (;;) {
@@ -439,13 +406,11 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
   };
 
   const int nch = (ne + kTetChunk - 1) / kTetChunk;
-  if (nch > 0) phase_a(0);
   for (int c = 0; c < nch; ++c) {
-    // stage c is complete and stage c + 1 is free (its last reader was phase B
-    // of chunk c - 1)
-    if (__syncthreads_or(kGuard && flag)) return false;
-    if (c + 1 < nch) phase_a(c + 1);
+    phase_a(c);
+    if (__syncthreads_or(kGuard && flag)) return false;   // stage c complete (or the patch goes native)
     phase_b(c);
+    __syncthreads();                                       // stage free for chunk c + 1
   }
   // ---- write the finished row: only its owner ever touched it, so no
   // barrier is needed; consecutive lanes write consecutive rows' k-th entries
@@ -457,7 +422,7 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
 }
 
 template <class T, class A, class RW>
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, 4)
 p1tet_laplace_fast_kernel(tm_patch_plan plan, tm_assemble_args args) {
   constexpr bool kGuard = std::is_same<A, L2>::value;
   using S = typename Ar<A>::S;
@@ -505,7 +470,7 @@ inline size_t p1tet_smem_bytes(const tm_patch_plan& plan, int coef_kind, size_t 
   const size_t nrp = (size_t)((plan.max_rows + 15) & ~15);
   size_t b = 32 + (size_t)plan.max_vtx * 3 * 8;
   if (coef_kind == TM_COEF_POINT) b += ((size_t)plan.max_vtx * 8 + 15) & ~size_t(15);
-  b += (size_t)plan.max_deg * nrp * elem + (size_t)2 * 10 * kTetChunk * elem;
+  b += (size_t)plan.max_deg * nrp * elem + (size_t)10 * kTetChunk * elem;
   return b;
 }
 

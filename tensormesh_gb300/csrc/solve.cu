@@ -32,7 +32,10 @@ struct PcgState {
   double bnorm;
 };
 
-__device__ __forceinline__ bool grid_sync(PcgState* st, unsigned nblocks, unsigned& my_gen) {
+constexpr long long kGridSpinLimit = 1ll << 25;  // ~1 s with the 32 ns back-off
+
+__device__ __forceinline__ bool grid_sync(PcgState* st, unsigned nblocks, unsigned& my_gen,
+                                          long long spin_limit = kGridSpinLimit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned g = my_gen;
@@ -46,7 +49,7 @@ __device__ __forceinline__ bool grid_sync(PcgState* st, unsigned nblocks, unsign
       volatile unsigned* gen = &st->gen;
       long long spins = 0;
       while (*gen == g) {
-        if (++spins > (1ll << 25)) {  // ~1 s with the 32 ns back-off
+        if (++spins > spin_limit) {
           atomicExch(&st->status, TM_ERR_TIMEOUT);
           break;
         }
@@ -754,4 +757,42 @@ extern "C" int tm_pcg_jacobi_noalloc(int64_t n, const int64_t* indptr, const int
   st = launch_pcg<float>(n, indptr, indices, values, b, x, rtol, atol, maxiter, static_cast<char*>(w), nb, s);
   if (st != TM_OK) return st;
   return tm_pcg_result(w, out_iters, out_res, nullptr, stream);
+}
+
+// ---------------------------------------------------------------------------
+// Self-test of the bounded grid barrier.  A cooperative launch in which CTA 0
+// returns without arriving: every other CTA's wait runs out after `spins`
+// polls (32 ns apart), the barrier records TM_ERR_TIMEOUT and every CTA
+// returns.  Nothing is left waiting, so the context stays usable.
+// ---------------------------------------------------------------------------
+namespace tmg {
+__global__ void barrier_timeout_kernel(PcgState* st, long long spins) {
+  unsigned gen = 0;
+  if (blockIdx.x == 0) return;  // the CTA that never arrives
+  grid_sync(st, gridDim.x, gen, spins);
+}
+}  // namespace tmg
+
+extern "C" int tm_selftest_barrier_timeout(int32_t n_blocks, int64_t spins, int32_t* out_status, void* work,
+                                           void* stream) {
+  if (out_status) *out_status = TM_OK;
+  if (n_blocks < 2 || spins < 1 || spins > tmg::kGridSpinLimit || !work || !out_status) return TM_ERR_INVALID;
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return TM_ERR_CUDA;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tmg::barrier_timeout_kernel, 32, 0);
+  if (n_blocks > sms * per_sm) return TM_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  tmg::PcgState* st = static_cast<tmg::PcgState*>(work);
+  if (cudaMemsetAsync(st, 0, sizeof(tmg::PcgState), s) != cudaSuccess) return TM_ERR_CUDA;
+  long long sp = spins;
+  void* args[] = {(void*)&st, (void*)&sp};
+  if (cudaLaunchCooperativeKernel((const void*)tmg::barrier_timeout_kernel, dim3(n_blocks), dim3(32), args, 0, s) !=
+      cudaSuccess)
+    return TM_ERR_CUDA;
+  tmg::PcgState h;
+  if (cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess) return TM_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return TM_ERR_CUDA;
+  *out_status = h.status;
+  return TM_OK;
 }

@@ -3,7 +3,8 @@
 This replaces the reference's ``from_mesh`` pattern build
 (assemble/element_assembler.py:838-875: scipy coo->csr->coo dedup of the
 element (row, col) pairs plus the per-entry slot map ``elem_eids``) with a
-device-side build in torch ops that produces:
+device-side build (the CSR pattern by the project's own kernels, the patch
+plan by torch ops) that produces:
 
 * the node-level CSR pattern (indptr, indices) in canonical order -- the
   same unique, row-major, column-sorted pairs the reference's ``edges`` hold;
@@ -44,7 +45,12 @@ class NodePattern:
 
 def node_pattern(elements: torch.Tensor, n_points: int) -> NodePattern:
     """Unique element (row, col) pairs in canonical CSR order
-    (element_assembler.py:838-866)."""
+    (element_assembler.py:838-866).  On a CUDA device the project's pattern
+    kernels build it (tm_pattern_count / tm_pattern_fill); a mesh kept on the
+    host (host-side planning and its unit tests) uses the same definition in
+    torch ops."""
+    if elements.is_cuda:
+        return _node_pattern_gpu(elements, n_points)
     E, B = elements.shape
     el = elements.long()
     u = el.unsqueeze(2).expand(E, B, B).reshape(-1)
@@ -57,6 +63,23 @@ def node_pattern(elements: torch.Tensor, n_points: int) -> NodePattern:
     indptr = torch.zeros(n_points + 1, dtype=torch.int64, device=elements.device)
     indptr[1:] = torch.cumsum(counts, 0)
     return NodePattern(n_points, indptr, cols.to(torch.int32), inv.view(E, B, B))
+
+
+def _node_pattern_gpu(elements: torch.Tensor, n_points: int) -> NodePattern:
+    E, B = elements.shape
+    dev = elements.device
+    el = elements.to(torch.int32).contiguous()
+    lib = _lib.load()
+    work = torch.empty(int(lib.tm_pattern_workspace_bytes(E, B, n_points)), dtype=torch.uint8, device=dev)
+    indptr = torch.empty(n_points + 1, dtype=torch.int64, device=dev)
+    stream = _lib.stream_handle(dev)
+    _lib.call("tm_pattern_count", el.data_ptr(), E, B, n_points, work.data_ptr(), indptr.data_ptr(), stream)
+    nnz = int(indptr[-1])
+    indices = torch.empty(nnz, dtype=torch.int32, device=dev)
+    slots = torch.empty((E, B, B), dtype=torch.int64, device=dev)
+    _lib.call("tm_pattern_fill", el.data_ptr(), E, B, n_points, work.data_ptr(), indptr.data_ptr(),
+              indices.data_ptr(), slots.data_ptr(), stream)
+    return NodePattern(n_points, indptr, indices, slots)
 
 
 def block_pattern(indptr: torch.Tensor, indices: torch.Tensor, H: int):

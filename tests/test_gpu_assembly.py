@@ -200,3 +200,27 @@ def test_high_valence_rows_match_oracle(ring):
             K = asm(mesh.points.to(dt), element_data={key: torch.tensor(kappa, dtype=dt, device=DEV)})
             assert np.array_equal(K.indptr.cpu().numpy(), ip) and np.array_equal(K.indices.cpu().numpy(), ix)
             assert rel_err(K.values.cpu().numpy(), dv) <= tol, (form, dt, precision)
+
+
+@pytest.mark.parametrize("etype", ETYPES)
+def test_pattern_kernels_match_host_definition(etype):
+    """tm_pattern_count / tm_pattern_fill: indptr, indices and the slot map
+    equal the host (torch) definition bit for bit, for shuffled element
+    orders and rows with more candidate columns than the kernel keeps in
+    registers (a 250-needle fan) or none at all (a node in no element)."""
+    from tensormesh_gb300.plan import node_pattern
+    base = tg.Mesh.gen_unit_square(13) if etype.startswith("tri") else tg.Mesh.gen_unit_cube(5)
+    mesh = base.to_p2() if etype.endswith(("6", "10")) else base
+    el = mesh.cells[etype]
+    perm = torch.randperm(el.shape[0], generator=torch.Generator().manual_seed(1))
+    cases = [(el, mesh.n_points), (el[perm], mesh.n_points)]
+    if etype == "tetra":
+        ring = 250
+        fan = torch.tensor([[0, 2 + k, 2 + (k + 1) % ring, 1] for k in range(ring)])
+        cases.append((fan, ring + 3))
+    for e, n in cases:
+        host = node_pattern(e, n)
+        dev = node_pattern(e.to(DEV), n)
+        assert torch.equal(dev.indptr.cpu(), host.indptr)
+        assert torch.equal(dev.indices.cpu(), host.indices)
+        assert torch.equal(dev.slots.cpu(), host.slots)

@@ -138,3 +138,27 @@ def test_clamped_elasticity_pipeline_matches_reference(golden_condense):
     assert rel_err(f_i.cpu(), g["c2/f_i"]) <= 1e-12
     u = cond.recover(K_ii.solve(f_i, rtol=1e-13))
     assert rel_err(u.cpu(), g["c2/u"]) <= 1e-9
+
+
+def test_bounded_grid_barrier_times_out_and_context_survives():
+    """The PCG kernels' grid barrier gives up instead of spinning: a
+    cooperative launch in which one CTA never arrives returns TM_ERR_TIMEOUT
+    (here after 2^20 polls), and the next solve on the same context works."""
+    import ctypes
+    from tensormesh_gb300 import _lib
+    lib = _lib.load()
+    work = torch.zeros(4096, dtype=torch.uint8, device=DEV)
+    status = ctypes.c_int32(-1)
+    st = lib.tm_selftest_barrier_timeout(8, 1 << 20, ctypes.byref(status), ctypes.c_void_p(work.data_ptr()),
+                                         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == _lib.TM_OK
+    assert status.value == _lib.TM_ERR_TIMEOUT
+    # a single CTA cannot wait on anyone: rejected before any launch
+    assert lib.tm_selftest_barrier_timeout(1, 1 << 20, ctypes.byref(status), ctypes.c_void_p(work.data_ptr()),
+                                           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)) == _lib.TM_ERR_INVALID
+    mesh = tg.Mesh.gen_unit_square(16, device=DEV)
+    K = tg.LaplaceElementAssembler.from_mesh(mesh, quadrature_order=1)(mesh.points)
+    b = tg.const_node_assembler(1.0).from_mesh(mesh, quadrature_order=1)(mesh.points)
+    K_ii, f_i = tg.Condenser(mesh.boundary_mask)(K, b)
+    K_ii.solve(f_i, rtol=1e-10)
+    assert K_ii.last_solve_info.status == 0 and K_ii.last_solve_info.residual <= 1e-10
