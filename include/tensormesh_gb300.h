@@ -322,6 +322,37 @@ int tm_pcg_jacobi(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t
 int tm_pcg_result(const void* work, int32_t* iters, double* res, double* bnorm, void* stream);
 
 /*
+ * The same Jacobi-PCG over a SELL-32 copy of the matrix (coalesced row
+ * slices, the preconditioner folded into the stored values).  method
+ * TM_PCG_STANDARD: the recurrence of tm_pcg_jacobi, two grid barriers per
+ * iteration; TM_PCG_PIPELINED: pipelined CG (Ghysels & Vanroose 2014), one
+ * barrier per iteration, whose recurrences lose accuracy faster (it can stop
+ * with TM_ERR_BREAKDOWN where the standard form converges).  Same stopping
+ * rule, statuses and meaning of x as tm_pcg_jacobi; the result is read back
+ * with tm_pcg_result on `work`.
+ *
+ * tm_sell_plan: slice pointers of the SELL-32 layout of an n-row CSR pattern,
+ * slice_ptr [ceil(n / 32) + 1] (device, int64): slice s holds rows
+ * 32 s .. 32 s + 31, padded to its longest row, entry j of row 32 s + l at
+ * slice_ptr[s] + 32 j + l.  Returns the padded entry count
+ * slice_ptr[ceil(n / 32)] (synchronises the stream), or -TM_ERR_* on error.
+ * The plan depends on the pattern only: compute it once per pattern.
+ *
+ * tm_pcg_jacobi_sell: work is caller-owned device scratch of at least
+ * tm_pcg_sell_workspace_bytes(dtype, n, n_pad) bytes (the SELL copy of the
+ * values, the preconditioned vectors, per-CTA partial sums).  A slice_ptr
+ * that does not cover every row returns TM_ERR_INDEX through tm_pcg_result
+ * (nothing is iterated).  Asynchronous on `stream`.
+ */
+int64_t tm_sell_plan(int64_t n, const int64_t* indptr, int64_t* slice_ptr, void* stream);
+int64_t tm_pcg_sell_workspace_bytes(int32_t dtype, int64_t n, int64_t n_pad);
+#define TM_PCG_STANDARD 0   /* Hestenes-Stiefel PCG, two grid barriers per iteration */
+#define TM_PCG_PIPELINED 1  /* Ghysels-Vanroose pipelined PCG, one barrier; less stable */
+int tm_pcg_jacobi_sell(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices, const void* values,
+                       const int64_t* slice_ptr, int64_t n_pad, const void* b, void* x, double rtol, double atol,
+                       int32_t maxiter, int32_t method, void* work, int64_t work_bytes, void* stream);
+
+/*
  * Allocation-free float32 Jacobi-PCG.  This entry point has no counterpart in
  * the reference.  It exists for callers that cannot allocate device memory
  * when they solve -- hosts that plan all device buffers up front, plugins

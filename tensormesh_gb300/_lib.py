@@ -18,6 +18,7 @@ TM_TRI3, TM_TRI6, TM_TET4, TM_TET10 = range(4)
 TM_FORM_LAPLACE, TM_FORM_MASS, TM_FORM_ELASTICITY, TM_FORM_LOAD = range(4)
 TM_F32, TM_F64 = 0, 1
 TM_PREC_EMULATED, TM_PREC_NATIVE = 0, 1
+TM_PCG_STANDARD, TM_PCG_PIPELINED = 0, 1
 TM_COEF_SCALAR, TM_COEF_ELEMENT, TM_COEF_POINT, TM_COEF_QUAD = range(4)
 
 STATUS_NAMES = {
@@ -38,6 +39,7 @@ EXPORTS = [
     "tm_mpnn_layer_bwd", "tm_mpnn_input_bwd", "tm_gather_axpy_f32",
     "tm_pcg_jacobi_noalloc", "tm_twolevel_apply", "tm_neohookean", "tm_facet_load",
     "tm_selftest_barrier_timeout", "tm_pattern_workspace_bytes", "tm_pattern_count", "tm_pattern_fill",
+    "tm_sell_plan", "tm_pcg_sell_workspace_bytes", "tm_pcg_jacobi_sell",
 ]
 
 P = ctypes.c_void_p
@@ -139,7 +141,13 @@ def _declare(lib):
         "tm_selftest_barrier_timeout": [i32, i64, ctypes.POINTER(i32), P, P],
         "tm_pattern_count": [P, i64, i32, i64, P, P, P],
         "tm_pattern_fill": [P, i64, i32, i64, P, P, P, P, P],
+        "tm_pcg_jacobi_sell": [i32, i64, P, P, P, P, i64, P, P, ctypes.c_double, ctypes.c_double, i32, i32, P, i64,
+                               P],
     }
+    lib.tm_sell_plan.argtypes = [i64, P, P, P]
+    lib.tm_sell_plan.restype = i64
+    lib.tm_pcg_sell_workspace_bytes.argtypes = [i32, i64, i64]
+    lib.tm_pcg_sell_workspace_bytes.restype = i64
     lib.tm_pattern_workspace_bytes.argtypes = [i64, i32, i64]
     lib.tm_pattern_workspace_bytes.restype = i64
     lib.tm_patch_smem_bytes.argtypes = [i32, i32, i32, i32, ctypes.POINTER(PatchPlan), i32, i32]

@@ -14,9 +14,16 @@ instance k (float32) and solves K_ii u_i = f_i (zero Dirichlet on each
 instance's boundary) with Jacobi-PCG -- all inside ONE kernel launch
 (``tm_batched_assemble_pcg``), captured in a CUDA graph and replayed.
 
-``autotune`` times the launch for cluster sizes x patch sizes and keeps the
-fastest; results are cached per (device, element, batch signature) in a JSON
-file (``TM_AUTOTUNE_CACHE`` or ~/.cache/tensormesh_gb300/autotune.json).
+Size-aware clusters: the batch time is set by its largest instances, whose
+PCG iterations are latency-bound on a small cluster, while the many small
+instances want many small clusters.  The ``n_big`` largest instances therefore
+run in a second persistent launch with ``cluster_big`` CTAs per cluster (8 or
+16, distributed shared memory across the cluster), concurrently on a forked
+stream with the launch that serves the rest; both are captured in the same
+CUDA graph.  ``autotune`` times the launch for patch sizes x cluster sizes x
+big-group shapes and keeps the fastest; results are cached per (device,
+element, batch signature) in a JSON file (``TM_AUTOTUNE_CACHE`` or
+~/.cache/tensormesh_gb300/autotune.json).
 """
 from __future__ import annotations
 
@@ -46,7 +53,8 @@ class BatchedPoisson:
     """Float32 assembly + Jacobi-PCG of independent P1 meshes in one launch."""
 
     def __init__(self, meshes: Sequence, quadrature_order: int = 1, source: float = 1.0,
-                 slot_budget: int = 2048, cluster: Optional[int] = None, device=None):
+                 slot_budget: int = 2048, cluster: Optional[int] = None, device=None,
+                 cluster_big: Optional[int] = None, n_big: int = 0):
         if not meshes:
             raise ValueError("empty batch")
         etypes = {m.default_element_type for m in meshes}
@@ -91,13 +99,14 @@ class BatchedPoisson:
         self.status = torch.empty(self.n_inst, dtype=torch.int32, device=dev)
         self.iters = torch.empty(self.n_inst, dtype=torch.int32, device=dev)
         self.resid = torch.empty(self.n_inst, dtype=torch.float32, device=dev)
-        self.queue = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.queue = torch.zeros(2, dtype=torch.int32, device=dev)   # one counter per launch group
         self.tables = E_.kernel_tables(self.element_type, quadrature_order, dev)
         self.kappa = torch.ones(self.n_elements, dtype=torch.float32, device=dev)
         self._plans = {}
         self._graph = None
         self._config = None
-        self.set_config(slot_budget, cluster)
+        self._side = None
+        self.set_config(slot_budget, cluster, cluster_big, n_big)
 
     # -- configuration ---------------------------------------------------------
     def _plan(self, slot_budget: int):
@@ -110,7 +119,11 @@ class BatchedPoisson:
             self._plans[slot_budget] = (plan, plan.to_struct(), pbeg.to(torch.int32))
         return self._plans[slot_budget]
 
-    def set_config(self, slot_budget: int, cluster: Optional[int]):
+    def set_config(self, slot_budget: int, cluster: Optional[int], cluster_big: Optional[int] = None,
+                   n_big: int = 0):
+        """Patch size, cluster size of the main launch, and the big group: the
+        ``n_big`` largest instances on clusters of ``cluster_big`` CTAs (no big
+        group when n_big is 0 or cluster_big is None)."""
         lib = _lib.load()
         plan, pstruct, pbeg = self._plan(slot_budget)
         chunk = 128
@@ -119,11 +132,26 @@ class BatchedPoisson:
                    lib.tm_patch_smem_bytes(self.el_id, _lib.TM_FORM_LOAD, 1, _lib.TM_F32, ctypes.byref(pstruct),
                                            _lib.TM_COEF_SCALAR, chunk))
         cluster = cluster or 4
-        n_clusters = lib.tm_batched_max_clusters(self.el_id, cluster, smem)
-        if n_clusters <= 0:
-            raise _lib.TensorMeshCudaError("tm_batched_max_clusters", -n_clusters if n_clusters < 0 else 6)
-        self._config = dict(slot_budget=slot_budget, cluster=cluster, n_clusters=n_clusters, smem=int(smem),
-                            chunk=chunk)
+        n_big = int(n_big) if cluster_big else 0
+        n_big = max(0, min(n_big, self.n_inst - 1))
+        cap = lib.tm_batched_max_clusters(self.el_id, cluster, smem)
+        if cap <= 0:
+            raise _lib.TensorMeshCudaError("tm_batched_max_clusters", -cap if cap < 0 else 6)
+        groups = []
+        if n_big > 0:
+            cap_big = lib.tm_batched_max_clusters(self.el_id, cluster_big, smem)
+            if cap_big <= 0:
+                raise _lib.TensorMeshCudaError("tm_batched_max_clusters", -cap_big if cap_big < 0 else 6)
+            nb = min(n_big, cap_big)
+            groups.append(dict(cluster=cluster_big, n_clusters=nb, first=0, count=n_big))
+            # the main launch takes the clusters the big group leaves free
+            used = -(-nb * cluster_big // cluster)
+            cap = max(1, cap - used)
+        groups.append(dict(cluster=cluster, n_clusters=cap, first=n_big, count=self.n_inst - n_big))
+        self._config = dict(slot_budget=slot_budget, cluster=cluster, n_clusters=groups[-1]["n_clusters"],
+                            cluster_big=cluster_big if n_big else None, n_big=n_big,
+                            n_clusters_big=groups[0]["n_clusters"] if n_big else 0, smem=int(smem), chunk=chunk)
+        self._groups = groups
         self._graph = None
         self._build_args(plan, pstruct, pbeg)
 
@@ -142,19 +170,22 @@ class BatchedPoisson:
         load.tables, load.points, load.coef = self.tables.data_ptr(), self.points.data_ptr(), 0
         load.scal[0] = self.source
         load.out = self.b.data_ptr()
-        a = _lib.BatchedArgs()
-        a.element, a.cluster, a.n_clusters, a.n_inst = self.el_id, cfg["cluster"], cfg["n_clusters"], self.n_inst
-        a.maxiter, a.chunk, a.rtol = 20000, cfg["chunk"], 1e-5
-        a.n_rows, a.smem_bytes = self.n_rows, cfg["smem"]
         self._keep = (pstruct, mat, load, plan, pbeg)
-        a.plan, a.mat, a.load = ctypes.pointer(pstruct), ctypes.pointer(mat), ctypes.pointer(load)
-        a.order, a.inst_pbeg, a.inst_rbeg = self.order.data_ptr(), pbeg.data_ptr(), self.inst_rbeg.data_ptr()
-        a.indices, a.dirichlet = self.pattern.indices.data_ptr(), self.dirichlet.data_ptr()
-        a.x, a.work = self.x.data_ptr(), self.work.data_ptr()
-        a.status, a.iters, a.resid, a.queue = (self.status.data_ptr(), self.iters.data_ptr(), self.resid.data_ptr(),
-                                               self.queue.data_ptr())
-        a.stream = 0
-        self._args = a
+        self._args = []
+        for gi, g in enumerate(self._groups):
+            a = _lib.BatchedArgs()
+            a.element, a.cluster, a.n_clusters, a.n_inst = self.el_id, g["cluster"], g["n_clusters"], g["count"]
+            a.maxiter, a.chunk, a.rtol = 20000, cfg["chunk"], 1e-5
+            a.n_rows, a.smem_bytes = self.n_rows, cfg["smem"]
+            a.plan, a.mat, a.load = ctypes.pointer(pstruct), ctypes.pointer(mat), ctypes.pointer(load)
+            a.order = self.order.data_ptr() + 4 * g["first"]
+            a.inst_pbeg, a.inst_rbeg = pbeg.data_ptr(), self.inst_rbeg.data_ptr()
+            a.indices, a.dirichlet = self.pattern.indices.data_ptr(), self.dirichlet.data_ptr()
+            a.x, a.work = self.x.data_ptr(), self.work.data_ptr()
+            a.status, a.iters, a.resid = self.status.data_ptr(), self.iters.data_ptr(), self.resid.data_ptr()
+            a.queue = self.queue.data_ptr() + 4 * gi
+            a.stream = 0
+            self._args.append(a)
 
     @property
     def config(self) -> dict:
@@ -166,14 +197,27 @@ class BatchedPoisson:
 
     # -- execution ---------------------------------------------------------------
     def launch(self, rtol: float = 1e-5, maxiter: int = 20000):
-        """One launch on the current stream (no host synchronisation)."""
-        self._args.rtol = float(rtol)
-        self._args.maxiter = int(maxiter)
-        _lib.call("tm_batched_assemble_pcg", ctypes.byref(self._args), _lib.stream_handle(self.device))
+        """The launch group(s) on the current stream (no host synchronisation):
+        with a big group, the main launch runs on a side stream forked from
+        and joined back into the current one, so the two overlap."""
+        cur = torch.cuda.current_stream(self.device)
+        for a in self._args:
+            a.rtol = float(rtol)
+            a.maxiter = int(maxiter)
+        if len(self._args) == 1:
+            _lib.call("tm_batched_assemble_pcg", ctypes.byref(self._args[0]), cur.cuda_stream)
+            return
+        if self._side is None:
+            self._side = torch.cuda.Stream(self.device)
+        self._side.wait_stream(cur)
+        _lib.call("tm_batched_assemble_pcg", ctypes.byref(self._args[0]), cur.cuda_stream)
+        with torch.cuda.stream(self._side):
+            _lib.call("tm_batched_assemble_pcg", ctypes.byref(self._args[1]), self._side.cuda_stream)
+        cur.wait_stream(self._side)
 
     def capture(self, rtol: float = 1e-5, maxiter: int = 20000) -> torch.cuda.CUDAGraph:
-        """Capture the launch in a CUDA graph (replayed by ``replay``)."""
-        self._args.rtol, self._args.maxiter = float(rtol), int(maxiter)
+        """Capture the launch group(s) in a CUDA graph (replayed by ``replay``)."""
+        self._captured_at = (float(rtol), int(maxiter))
         s = torch.cuda.Stream(self.device)
         s.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(s):
@@ -197,7 +241,7 @@ class BatchedPoisson:
             raise AssertionError(f"kappa must have {self.n_elements} entries, got {kappa.shape[0]}")
         self.kappa.copy_(kappa.to(self.device, torch.float32))
         if graph:
-            if self._graph is None or self._args.rtol != float(rtol) or self._args.maxiter != int(maxiter):
+            if self._graph is None or self._captured_at != (float(rtol), int(maxiter)):
                 self.capture(rtol, maxiter)
             self._graph.replay()
         else:
@@ -213,41 +257,46 @@ class BatchedPoisson:
         h.update(f"{self.element_type}|{self.n_inst}|{self.n_rows}|{self.n_elements}".encode())
         return h.hexdigest()[:16]
 
-    def autotune(self, kappa: torch.Tensor, clusters=(1, 2, 4, 8), budgets=(1024, 2048, 4096), reps: int = 3,
-                 rtol: float = 1e-5, use_cache: bool = True) -> dict:
-        """Time every (cluster, slot budget) candidate on this batch and keep
-        the fastest.  Returns the chosen config with its time in ms."""
+    def autotune(self, kappa: torch.Tensor, clusters=(2, 4, 8), budgets=(1024, 2048, 4096), reps: int = 3,
+                 rtol: float = 1e-5, use_cache: bool = True, big=((None, 0), (8, 4), (16, 2), (16, 8))) -> dict:
+        """Time every (slot budget, cluster, big group) candidate on this batch
+        and keep the fastest; ``big`` lists (cluster_big, n_big) shapes,
+        (None, 0) being a single launch.  Returns the chosen config with its
+        time in ms."""
         name = torch.cuda.get_device_name(self.device)
-        key = f"batched|{name}|{self.signature()}|{rtol}"
+        key = f"batched2|{name}|{self.signature()}|{rtol}"
         if use_cache:
             hit = _load_cache().get(key)
             if hit:
-                self.set_config(hit["slot_budget"], hit["cluster"])
+                self.set_config(hit["slot_budget"], hit["cluster"], hit.get("cluster_big"), hit.get("n_big", 0))
                 return hit
         self.kappa.copy_(kappa.to(self.device, torch.float32))
         results = []
         for bgt in budgets:
             for cl in clusters:
-                try:
-                    self.set_config(bgt, cl)
-                    self.launch(rtol)
-                    torch.cuda.synchronize(self.device)
-                    e0 = torch.cuda.Event(enable_timing=True)
-                    e1 = torch.cuda.Event(enable_timing=True)
-                    e0.record()
-                    for _ in range(reps):
+                for cb, nbig in big:
+                    try:
+                        self.set_config(bgt, cl, cb, nbig)
                         self.launch(rtol)
-                    e1.record()
-                    torch.cuda.synchronize(self.device)
-                    results.append((e0.elapsed_time(e1) / reps, bgt, cl))
-                except _lib.TensorMeshCudaError:
-                    continue
+                        torch.cuda.synchronize(self.device)
+                        e0 = torch.cuda.Event(enable_timing=True)
+                        e1 = torch.cuda.Event(enable_timing=True)
+                        e0.record()
+                        for _ in range(reps):
+                            self.launch(rtol)
+                        e1.record()
+                        torch.cuda.synchronize(self.device)
+                        results.append((e0.elapsed_time(e1) / reps, bgt, cl, cb or 0, nbig if cb else 0))
+                    except _lib.TensorMeshCudaError:
+                        continue
         if not results:
             raise RuntimeError("autotune: no launch configuration ran")
-        ms, bgt, cl = min(results)
-        self.set_config(bgt, cl)
-        best = dict(slot_budget=bgt, cluster=cl, ms=ms, n_clusters=self._config["n_clusters"],
-                    candidates=[dict(ms=r[0], slot_budget=r[1], cluster=r[2]) for r in results])
+        ms, bgt, cl, cb, nbig = min(results)
+        self.set_config(bgt, cl, cb or None, nbig)
+        best = dict(slot_budget=bgt, cluster=cl, cluster_big=cb or None, n_big=nbig, ms=ms,
+                    n_clusters=self._config["n_clusters"], n_clusters_big=self._config["n_clusters_big"],
+                    candidates=[dict(ms=r[0], slot_budget=r[1], cluster=r[2], cluster_big=r[3] or None, n_big=r[4])
+                                for r in results])
         if use_cache:
             _store_cache(key, best)
         return best

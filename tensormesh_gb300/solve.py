@@ -120,17 +120,53 @@ class PCGWorkspace:
         self.n, self.nnz, self.dtype = n, nnz, dtype
 
 
+class SellWorkspace:
+    """Device scratch for tm_pcg_jacobi_sell (n rows, n_pad SELL-32 entries)."""
+
+    def __init__(self, n: int, n_pad: int, dtype: torch.dtype, device):
+        lib = _lib.load()
+        code = _lib.TM_F64 if dtype == torch.float64 else _lib.TM_F32
+        self.nbytes = int(lib.tm_pcg_sell_workspace_bytes(code, n, n_pad))
+        if self.nbytes < 0:
+            raise _lib.TensorMeshCudaError("tm_pcg_sell_workspace_bytes", -self.nbytes)
+        self.buf = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
+
+
 _WS = {}
 
 
-def workspace(n, nnz, dtype, device) -> PCGWorkspace:
-    key = (n, nnz, dtype, str(device))
+def _cached(key, make):
     ws = _WS.get(key)
     if ws is None:
         if len(_WS) > 4:
             _WS.clear()
-        ws = _WS[key] = PCGWorkspace(n, nnz, dtype, device)
+        ws = _WS[key] = make()
     return ws
+
+
+def workspace(n, nnz, dtype, device) -> PCGWorkspace:
+    return _cached(("csr", n, nnz, dtype, str(device)), lambda: PCGWorkspace(n, nnz, dtype, device))
+
+
+def sell_plan(indptr: torch.Tensor):
+    """(slice_ptr, n_pad) of the SELL-32 layout of a CSR pattern (tm_sell_plan),
+    cached on the indptr tensor while it is unmodified."""
+    cached = getattr(indptr, "_tm_sell", None)
+    if cached is not None and cached[0] == indptr._version:
+        return cached[1], cached[2]
+    n = indptr.shape[0] - 1
+    sp = torch.empty((n + 31) // 32 + 1, dtype=torch.int64, device=indptr.device)
+    n_pad = int(_lib.load().tm_sell_plan(n, indptr.data_ptr(), sp.data_ptr(), _lib.stream_handle(indptr.device)))
+    if n_pad < 0:
+        raise _lib.TensorMeshCudaError("tm_sell_plan", -n_pad)
+    indptr._tm_sell = (indptr._version, sp, n_pad)
+    return sp, n_pad
+
+
+# "sell": standard PCG over the SELL-32 copy (tm_pcg_jacobi_sell); "sell-pipelined":
+# the one-barrier pipelined form over the same copy (a breakdown restarts it
+# from the current iterate); "csr": the CSR kernel (tm_pcg_jacobi).
+LAYOUT = "sell"
 
 
 def pcg_jacobi_raw(indptr, indices, values, b, x, rtol=1e-8, atol=0.0, maxiter=100000, max_restarts=5):
@@ -145,9 +181,24 @@ def pcg_jacobi_raw(indptr, indices, values, b, x, rtol=1e-8, atol=0.0, maxiter=1
     accuracy the remaining gap needs, and x += d."""
     n = b.shape[0]
     dev = values.device
-    ws = workspace(n, int(values.shape[0]), values.dtype, dev)
     s = _lib.stream_handle(dev)
     code = _dt(values)
+    pipelined = LAYOUT == "sell-pipelined"
+    if LAYOUT in ("sell", "sell-pipelined"):
+        sp, n_pad = sell_plan(indptr)
+        ws = _cached(("sell", n, n_pad, values.dtype, str(dev)), lambda: SellWorkspace(n, n_pad, values.dtype, dev))
+        method = _lib.TM_PCG_PIPELINED if pipelined else _lib.TM_PCG_STANDARD
+
+        def launch(rhs, sol, rt, at, budget):
+            _lib.call("tm_pcg_jacobi_sell", code, n, indptr.data_ptr(), indices.data_ptr(), values.data_ptr(),
+                      sp.data_ptr(), n_pad, rhs.data_ptr(), sol.data_ptr(), rt, at, budget, method,
+                      ws.buf.data_ptr(), ws.nbytes, s)
+    else:
+        ws = workspace(n, int(values.shape[0]), values.dtype, dev)
+
+        def launch(rhs, sol, rt, at, budget):
+            _lib.call("tm_pcg_jacobi", code, n, indptr.data_ptr(), indices.data_ptr(), values.data_ptr(),
+                      rhs.data_ptr(), sol.data_ptr(), rt, at, budget, ws.buf.data_ptr(), ws.nbytes, s)
     bnorm = float(torch.linalg.vector_norm(b.double()))
     target = max(rtol, atol / max(bnorm, 1e-300))
     total_it = 0
@@ -156,22 +207,21 @@ def pcg_jacobi_raw(indptr, indices, values, b, x, rtol=1e-8, atol=0.0, maxiter=1
     rhs, sol, inner_rtol, inner_atol = b, x, float(rtol), float(atol)
     while True:
         budget = max(0, maxiter - total_it)
-        _lib.call("tm_pcg_jacobi", code, n, indptr.data_ptr(), indices.data_ptr(), values.data_ptr(),
-                  rhs.data_ptr(), sol.data_ptr(), inner_rtol, inner_atol, int(budget), ws.buf.data_ptr(),
-                  ws.nbytes, s)
+        launch(rhs, sol, inner_rtol, inner_atol, int(budget))
         it = _lib.ctypes.c_int32(0)
         res = _lib.ctypes.c_double(0.0)
         bn = _lib.ctypes.c_double(0.0)
         status = _lib.load().tm_pcg_result(ws.buf.data_ptr(), _lib.ctypes.byref(it), _lib.ctypes.byref(res),
                                            _lib.ctypes.byref(bn), s)
         total_it += it.value
-        if status == _lib.TM_ERR_TIMEOUT or status == _lib.TM_ERR_CUDA:
+        if status in (_lib.TM_ERR_TIMEOUT, _lib.TM_ERR_CUDA, _lib.TM_ERR_INDEX):
             raise _lib.TensorMeshCudaError("tm_pcg_jacobi", status)
         if sol is not x:
             x.add_(sol)
         true_res = true_relative_residual(indptr, indices, values, b, x, bnorm)
         info = SolveInfo(status, total_it, true_res, res.value / max(bnorm, 1e-300), restarts)
-        if status != _lib.TM_OK or true_res <= target * 1.0000001 or restarts >= max_restarts or total_it >= maxiter:
+        retry = status == _lib.TM_OK or (pipelined and status == _lib.TM_ERR_BREAKDOWN)
+        if not retry or true_res <= target * 1.0000001 or restarts >= max_restarts or total_it >= maxiter:
             return info
         restarts += 1
         rhs = (b - spmv_raw(indptr, indices, values, x)).contiguous()
