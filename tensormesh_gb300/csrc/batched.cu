@@ -341,6 +341,7 @@ extern "C" int64_t tm_patch_smem_bytes(int32_t element, int32_t form, int32_t n_
 }
 
 extern "C" int tm_batched_max_clusters(int32_t element, int32_t cluster, int64_t smem_bytes) {
+  if (cluster < 1 || cluster > 16) return -TM_ERR_INVALID;
   cudaLaunchConfig_t cfg = {};
   cfg.blockDim = dim3(tmg::kBatchThreads);
   cfg.dynamicSmemBytes = (size_t)smem_bytes;
@@ -354,13 +355,20 @@ extern "C" int tm_batched_max_clusters(int32_t element, int32_t cluster, int64_t
   cfg.numAttrs = 1;
   int n = 0;
   cudaError_t e;
+  // clusters above the portable size 8 must be allowed before the query
   if (element == TM_TRI3) {
     cudaFuncSetAttribute(tmg::batched_assemble_pcg_kernel<TM_TRI3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem_bytes);
+    if (cluster > 8)
+      cudaFuncSetAttribute(tmg::batched_assemble_pcg_kernel<TM_TRI3>,
+                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     e = cudaOccupancyMaxActiveClusters(&n, tmg::batched_assemble_pcg_kernel<TM_TRI3>, &cfg);
   } else if (element == TM_TET4) {
     cudaFuncSetAttribute(tmg::batched_assemble_pcg_kernel<TM_TET4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem_bytes);
+    if (cluster > 8)
+      cudaFuncSetAttribute(tmg::batched_assemble_pcg_kernel<TM_TET4>,
+                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     e = cudaOccupancyMaxActiveClusters(&n, tmg::batched_assemble_pcg_kernel<TM_TET4>, &cfg);
   } else {
     return -TM_ERR_UNSUPPORTED;

@@ -240,6 +240,7 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
   }
   const int kf = fr.k;
   const ShortConv sconv = short_conv(fr.t + fr.z - 62);
+  const double esc_native = std::is_same<A, double>::value ? ldexp(1.0, fr.z - 62) : 0.0;
   const T* coef = static_cast<const T*>(args.coef);
   if (args.coef_kind == TM_COEF_POINT)
     for (int i = tid; i < nv; i += kThreads) s_pc[i] = P::st(P::in(coef[plan.vtx[vbeg + i]]));
@@ -315,6 +316,15 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
 #pragma unroll
         for (int k = 0; k < 3; ++k) d[k][j] = P::pair(sconv(r32[2 * (lv[k + 1] * 3 + j)] - r0), 0.f);
       }
+      e_sh = 0;
+    } else if constexpr (std::is_same<A, double>::value) {
+      // native FP64 (patches handed over by the guard): the full 53 bits of
+      // every difference, in frame units (a 48-bit split would carry its
+      // 2^-48 error through these ill-conditioned elements)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) d[k][j] = __ll2double_rn(s_R[lv[k + 1] * 3 + j] - s_R[lv[0] * 3 + j]) * esc_native;
       e_sh = 0;
     } else {
       float eh[3][3], el[3][3];

@@ -21,12 +21,16 @@ def make_batch(sizes, seed=0):
 
 
 @pytest.mark.parametrize("graph", [False, True])
-@pytest.mark.parametrize("cluster", [1, 4])
-def test_batched_matches_fp64_oracle(graph, cluster, tmp_path, monkeypatch):
+@pytest.mark.parametrize("cluster,big", [(1, None), (4, None), (2, (8, 2)), (2, (16, 1))])
+def test_batched_matches_fp64_oracle(graph, cluster, big, tmp_path, monkeypatch):
+    """big = (cluster_big, n_big): the largest instances run in a second,
+    concurrent launch on larger clusters."""
     monkeypatch.setenv("TM_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
     sizes = [5, 17, 32, 9, 24, 3]
     meshes, kappas = make_batch(sizes)
-    bp = BatchedPoisson(meshes, cluster=cluster)
+    cb, nbig = big if big else (None, 0)
+    bp = BatchedPoisson(meshes, cluster=cluster, cluster_big=cb, n_big=nbig)
+    assert bp.config["n_big"] == nbig
     k = torch.cat(kappas).to(DEV)
     u, info = bp(k, rtol=1e-6, graph=graph)
     torch.cuda.synchronize()
@@ -48,10 +52,12 @@ def test_batched_matches_fp64_oracle(graph, cluster, tmp_path, monkeypatch):
             assert np.max(np.abs(uu - uref)) <= 5e-4 * np.max(np.abs(uref))
 
 
-def test_batched_graph_replay_is_deterministic(tmp_path, monkeypatch):
+@pytest.mark.parametrize("big", [None, (8, 1)])
+def test_batched_graph_replay_is_deterministic(big, tmp_path, monkeypatch):
     monkeypatch.setenv("TM_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
     meshes, kappas = make_batch([12, 30, 7, 20], seed=1)
-    bp = BatchedPoisson(meshes, cluster=2)
+    cb, nbig = big if big else (None, 0)
+    bp = BatchedPoisson(meshes, cluster=2, cluster_big=cb, n_big=nbig)
     k = torch.cat(kappas).to(DEV)
     u1, _ = bp(k)
     a = u1.clone()
@@ -66,11 +72,13 @@ def test_autotuner_picks_and_caches(tmp_path, monkeypatch):
     meshes, kappas = make_batch([10, 40, 25], seed=2)
     bp = BatchedPoisson(meshes)
     k = torch.cat(kappas).to(DEV)
-    best = bp.autotune(k, clusters=(1, 2, 4), budgets=(512, 2048), reps=2)
+    best = bp.autotune(k, clusters=(1, 2, 4), budgets=(512, 2048), reps=2, big=((None, 0), (8, 1)))
     assert best["cluster"] in (1, 2, 4) and best["slot_budget"] in (512, 2048)
+    assert len(best["candidates"]) == 12
     assert path.exists()
     bp2 = BatchedPoisson(meshes)
-    again = bp2.autotune(k, clusters=(1, 2, 4), budgets=(512, 2048))
+    again = bp2.autotune(k, clusters=(1, 2, 4), budgets=(512, 2048), big=((None, 0), (8, 1)))
     assert again["cluster"] == best["cluster"] and bp2.config["slot_budget"] == best["slot_budget"]
+    assert bp2.config["n_big"] == best["n_big"]
     u, info = bp2(k)
     assert int(info.status.max()) == 0
