@@ -294,7 +294,7 @@ def run_ours(args):
         return a.elapsed_time(b_) / reps
 
     fp32 = None
-    if not args.no_extra:
+    if want_extra(args, "fp32"):
         pts32 = mesh.points.float().contiguous()
         kap32 = kappa.float()
         asm32 = KappaLaplace.from_assembler(asm)
@@ -310,7 +310,7 @@ def run_ours(args):
 
     # ---- boundary traction load (FacetAssembler) on the same 128^3 mesh, FP64
     facet = None
-    if not args.no_extra:
+    if want_extra(args, "facet"):
         class Traction(tg.FacetAssembler):
             def forward(self, v):
                 return v[:, None] * torch.tensor([0.0, 0.3, -1.0], dtype=v.dtype, device=v.device)
@@ -329,7 +329,7 @@ def run_ours(args):
     # ---- 64^3 P1-tet linear elasticity, per-element E, FP64 (secondary)
     elast = None
     hyper = None
-    if not args.no_extra:
+    if want_extra(args, "elasticity"):
         m2 = tg.Mesh.gen_unit_cube(64, device=dev)
         rng = np.random.default_rng(SEED + 2)
         Emod = torch.from_numpy(np.exp(0.5 * rng.normal(size=m2.n_elements))).to(dev)
@@ -386,7 +386,7 @@ def run_ours(args):
     #      split square, FP64 (forward assembly + Jacobi-PCG + adjoint solve +
     #      backward assembly)
     adjoint = None
-    if not args.no_extra:
+    if want_extra(args, "adjoint"):
         m4 = tg.Mesh.gen_unit_square(256, device=dev)
         k4 = torch.from_numpy(np.exp(np.random.default_rng(SEED + 4).normal(size=m4.n_elements))).to(dev)
         a4 = KappaLaplace.from_mesh(m4, quadrature_order=1)
@@ -424,7 +424,7 @@ def run_ours(args):
     # ---- 256 uneven 2D Poisson meshes, assembled + Jacobi-PCG in one
     #      persistent, graph-captured launch (FP32), autotuned launch shape
     batched = None
-    if not args.no_extra:
+    if want_extra(args, "batched"):
         from tensormesh_gb300.batched import BatchedPoisson
         rng = np.random.default_rng(SEED + 3)
         sizes = rng.integers(32, 257, size=256)
@@ -616,6 +616,17 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+EXTRAS = ("fp32", "facet", "elasticity", "adjoint", "batched")
+
+
+def want_extra(args, name: str) -> bool:
+    """Whether the side measurement ``name`` runs: all of them by default,
+    none with --no-extra, a comma-separated subset with --extra."""
+    if args.no_extra:
+        return False
+    return args.extra is None or name in args.extra.split(",")
+
+
 def hbm_peak():
     """(GB/s, "measured" | "fallback"): the copy bandwidth in MEASURED_PEAKS.json,
     else the fallback figure of an earlier GB300 measurement."""
@@ -636,7 +647,9 @@ def main():
     ap.add_argument("--cube", type=int, default=N_CELLS, help="cells per side (profiling runs use smaller cubes)")
     ap.add_argument("--pcg-maxiter", type=int, default=200000)
     ap.add_argument("--no-learned", action="store_true")
-    ap.add_argument("--no-extra", action="store_true", help="skip the float32 and elasticity side measurements")
+    ap.add_argument("--no-extra", action="store_true", help="skip every side measurement")
+    ap.add_argument("--extra", default=None,
+                    help="comma-separated side measurements to run, of " + ",".join(EXTRAS) + " (default: all)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--slot-budget", type=int, default=0, help="fixed patch slot budget instead of autotuning")
     args = ap.parse_args()

@@ -336,6 +336,8 @@ int tm_pcg_result(const void* work, int32_t* iters, double* res, double* bnorm, 
  * 32 s .. 32 s + 31, padded to its longest row, entry j of row 32 s + l at
  * slice_ptr[s] + 32 j + l.  Returns the padded entry count
  * slice_ptr[ceil(n / 32)] (synchronises the stream), or -TM_ERR_* on error.
+ * out_narrow (host, may be NULL) is set to 1 when every |column - row| <= 32767:
+ * the solve may then pass TM_PCG_NARROW and store 16-bit column offsets.
  * The plan depends on the pattern only: compute it once per pattern.
  *
  * tm_pcg_jacobi_sell: work is caller-owned device scratch of at least
@@ -344,10 +346,13 @@ int tm_pcg_result(const void* work, int32_t* iters, double* res, double* bnorm, 
  * that does not cover every row returns TM_ERR_INDEX through tm_pcg_result
  * (nothing is iterated).  Asynchronous on `stream`.
  */
-int64_t tm_sell_plan(int64_t n, const int64_t* indptr, int64_t* slice_ptr, void* stream);
+int64_t tm_sell_plan(int64_t n, const int64_t* indptr, const int32_t* indices, int64_t* slice_ptr,
+                     int32_t* out_narrow, void* stream);
 int64_t tm_pcg_sell_workspace_bytes(int32_t dtype, int64_t n, int64_t n_pad);
 #define TM_PCG_STANDARD 0   /* Hestenes-Stiefel PCG, two grid barriers per iteration */
 #define TM_PCG_PIPELINED 1  /* Ghysels-Vanroose pipelined PCG, one barrier; less stable */
+#define TM_PCG_NARROW 2     /* or-ed in: 16-bit column offsets (the plan's out_narrow must be 1;
+                               an offset that does not fit returns TM_ERR_INDEX) */
 int tm_pcg_jacobi_sell(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices, const void* values,
                        const int64_t* slice_ptr, int64_t n_pad, const void* b, void* x, double rtol, double atol,
                        int32_t maxiter, int32_t method, void* work, int64_t work_bytes, void* stream);

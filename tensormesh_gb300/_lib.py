@@ -18,7 +18,7 @@ TM_TRI3, TM_TRI6, TM_TET4, TM_TET10 = range(4)
 TM_FORM_LAPLACE, TM_FORM_MASS, TM_FORM_ELASTICITY, TM_FORM_LOAD = range(4)
 TM_F32, TM_F64 = 0, 1
 TM_PREC_EMULATED, TM_PREC_NATIVE = 0, 1
-TM_PCG_STANDARD, TM_PCG_PIPELINED = 0, 1
+TM_PCG_STANDARD, TM_PCG_PIPELINED, TM_PCG_NARROW = 0, 1, 2
 TM_COEF_SCALAR, TM_COEF_ELEMENT, TM_COEF_POINT, TM_COEF_QUAD = range(4)
 
 STATUS_NAMES = {
@@ -144,7 +144,7 @@ def _declare(lib):
         "tm_pcg_jacobi_sell": [i32, i64, P, P, P, P, i64, P, P, ctypes.c_double, ctypes.c_double, i32, i32, P, i64,
                                P],
     }
-    lib.tm_sell_plan.argtypes = [i64, P, P, P]
+    lib.tm_sell_plan.argtypes = [i64, P, P, P, ctypes.POINTER(i32), P]
     lib.tm_sell_plan.restype = i64
     lib.tm_pcg_sell_workspace_bytes.argtypes = [i32, i64, i64]
     lib.tm_pcg_sell_workspace_bytes.restype = i64

@@ -92,4 +92,56 @@ TM_D df64 ld2(const F2* a, int64_t i) {
 }
 TM_D void st2(F2* a, int64_t i, df64 v) { a[i] = F2{v.hi, v.lo}; }
 
+// Two per-CTA sums at once (one pass of shuffles and one of barriers), for
+// CTAs of at most 16 warps (s_red holds 32 doubles); valid in thread 0.
+__device__ __forceinline__ void block_sum2(double& a, double& b, double* s_red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  if (lane == 0) {
+    s_red[warp] = a;
+    s_red[16 + warp] = b;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    a = lane < nw ? s_red[lane] : 0.0;
+    b = lane < nw ? s_red[16 + lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+  }
+  __syncthreads();
+}
+
+// The sums of two partial arrays (same order in every CTA), in one pass.
+__device__ __forceinline__ void sum_partials2(const double* pa, const double* pb, int n, double* s_red, double& a,
+                                              double& b) {
+  if (threadIdx.x < 32) {
+    double va = 0.0, vb = 0.0;
+    for (int i = threadIdx.x; i < n; i += 32) {
+      va += ((volatile const double*)pa)[i];
+      vb += ((volatile const double*)pb)[i];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      va += __shfl_down_sync(0xffffffffu, va, o);
+      vb += __shfl_down_sync(0xffffffffu, vb, o);
+    }
+    if (threadIdx.x == 0) {
+      s_red[0] = va;
+      s_red[1] = vb;
+    }
+  }
+  __syncthreads();
+  a = s_red[0];
+  b = s_red[1];
+  __syncthreads();
+}
+
 }  // namespace tmg

@@ -73,6 +73,28 @@ template <> struct SellT<F2> {
   static TM_D A zero() { return {0.f, 0.f}; }
 };
 
+// Column of a stored entry: absolute (int32) or relative to the row (int16,
+// for matrices whose every |column - row| fits; FEM orderings keep the
+// coupling bandwidth small), the latter saving 2 of the 12 bytes an entry
+// streams per iteration.
+TM_D int col_of(const int32_t* scol, int64_t k, int64_t) { return __ldg(scol + k); }
+TM_D int col_of(const int16_t* scol, int64_t k, int64_t row) { return (int)row + (int)__ldg(scol + k); }
+
+// Largest |column - row| of the matrix (atomic max into *span).
+__global__ void sell_span_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ idx,
+                                 unsigned long long* span) {
+  const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  unsigned long long m = 0ull;
+  if (row < n)
+    for (int64_t k = indptr[row]; k < indptr[row + 1]; ++k) {
+      const long long d = (long long)idx[k] - row;
+      m = max(m, (unsigned long long)(d < 0 ? -d : d));
+    }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(span, m);
+}
+
 // Slice widths (32 x the longest row of each slice) into sptr[1..n_slices].
 __global__ void sell_width_kernel(int64_t n, const int64_t* __restrict__ indptr, int64_t* __restrict__ sptr) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -135,12 +157,13 @@ __global__ void sell_dinv_kernel(int64_t n, const int64_t* __restrict__ indptr, 
 // warp per slice, lane l on row 32 s + l.  A slice plan that does not cover
 // its rows (width < 32 x row length, or a range outside [0, n_pad]) raises
 // TM_ERR_INDEX in the solver record instead of writing.
-template <class S>
+template <class S, class CT>
 __global__ void sell_fill_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ idx,
                                  const typename SellT<S>::V* __restrict__ val, const int64_t* __restrict__ sptr,
                                  int64_t n_pad, const S* __restrict__ dinv, const typename SellT<S>::V* __restrict__ x0,
-                                 int32_t* __restrict__ scol, S* __restrict__ sval, S* __restrict__ y,
+                                 CT* __restrict__ scol, S* __restrict__ sval, S* __restrict__ y,
                                  PcgState* st) {
+  constexpr bool kRel = sizeof(CT) == 2;
   using Tr = SellT<S>;
   using A = typename Tr::A;
   const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -158,7 +181,10 @@ __global__ void sell_fill_kernel(int64_t n, const int64_t* __restrict__ indptr, 
   }
   const int L = (int)(width >> 5);
   const int64_t base = row < n ? indptr[row] : 0;
-  const int32_t pad_col = row < n ? (int32_t)row : 0;
+  // pad entries gather a valid column: the row itself, or the last row for
+  // the lanes past n of the last slice
+  const int32_t pad_col = row < n ? (int32_t)row : (int32_t)(n - 1);
+  bool wide = false;
   for (int j = 0; j < L; ++j) {
     const int64_t k = s0 + (int64_t)j * 32 + lane;
     int32_t c = pad_col;
@@ -167,17 +193,24 @@ __global__ void sell_fill_kernel(int64_t n, const int64_t* __restrict__ indptr, 
       c = idx[base + j];
       v = Tr::in(val[base + j]) * Tr::ld(dinv, c);
     }
-    scol[k] = c;
+    if constexpr (kRel) {
+      const long long d = (long long)c - row;
+      wide = wide || d < -32768 || d > 32767;
+      scol[k] = (CT)d;
+    } else {
+      scol[k] = c;
+    }
     sval[k] = Tr::pack(v);
   }
+  if (kRel && __any_sync(0xffffffffu, wide) && lane == 0) atomicExch(&st->status, TM_ERR_INDEX);
   if (row < n) Tr::st(y, row, Tr::in(x0[row]) / Tr::ld(dinv, row));
 }
 
 // acc[u] = sum_j sval[.] * g(scol[.]) over the rows of slices sl + u * kSellWarps
 // (u < kSellRows) of [sl, s_hi), for the calling lane's row.  g gathers the
 // operand's column value (one vector, or a combination of two).
-template <class S, class G>
-TM_D void sell_rows(const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol, const S* __restrict__ sval,
+template <class S, class CT, class G>
+TM_D void sell_rows(const int64_t* __restrict__ sptr, const CT* __restrict__ scol, const S* __restrict__ sval,
                     const G& g, int64_t sl, int64_t s_hi, typename SellT<S>::A (&acc)[kSellRows]) {
   using Tr = SellT<S>;
   const int lane = threadIdx.x & 31;
@@ -202,7 +235,7 @@ TM_D void sell_rows(const int64_t* __restrict__ sptr, const int32_t* __restrict_
       for (int j = 0; j < kSellIlp; ++j) {
         const bool ok = j0 + j < len[u];
         const int64_t k = off[u] + (int64_t)(j0 + j) * 32;
-        c[u][j] = ok ? __ldg(scol + k) : 0;
+        c[u][j] = ok ? col_of(scol, k, (sl + (int64_t)u * kSellWarps) * 32 + lane) : 0;
         v[u][j] = ok ? sval[k] : S{};
       }
 #pragma unroll
@@ -222,9 +255,9 @@ TM_D void sell_rows(const int64_t* __restrict__ sptr, const int32_t* __restrict_
 //            rz = sum M r^2 and rr = sum r^2                        [barrier]
 // The iterates are those of tm_pcg_jacobi's recurrence (z = M r, p = z +
 // beta p), so its rounding behaviour is that of standard PCG.
-template <class S>
+template <class S, class CT>
 __global__ void __launch_bounds__(kSellThreads, 2)
-pcg_sell_hs_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
+pcg_sell_hs_kernel(int64_t n, const int64_t* __restrict__ sptr, const CT* __restrict__ scol,
                    const S* __restrict__ sval, const S* __restrict__ dinv, const typename SellT<S>::V* __restrict__ bv,
                    typename SellT<S>::V* __restrict__ xv, S* x, S* r, S* q, S* pt0, S* pt1, const S* y,
                    double* partials, PcgState* st, double rtol, double atol, int maxiter) {
@@ -243,9 +276,13 @@ pcg_sell_hs_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* _
   double* pC = partials + 2 * (int64_t)nb;
   auto row_of = [&](int64_t sl, int u) { return (sl + (int64_t)u * kSellWarps) * 32 + lane; };
   auto valid = [&](int64_t sl, int u) { return sl + (int64_t)u * kSellWarps < s_hi && row_of(sl, u) < n; };
-  auto publish = [&](double* dst, A v) {
-    const double t = block_sum(Tr::to_double(v), s_red);
-    if (threadIdx.x == 0) dst[blockIdx.x] = t;
+  auto publish2 = [&](double* da, A va, double* db, A vb) {
+    double a = Tr::to_double(va), b = Tr::to_double(vb);
+    block_sum2(a, b, s_red);
+    if (threadIdx.x == 0) {
+      da[blockIdx.x] = a;
+      db[blockIdx.x] = b;
+    }
   };
 
   // ---- r = b - (A M) y, x = x0, pt_old = 0; rz, rr, bb
@@ -253,7 +290,7 @@ pcg_sell_hs_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* _
     A rz_l = Tr::zero(), rr_l = Tr::zero(), bb_l = Tr::zero();
     for (int64_t sl = s_lo + warp; sl < s_hi; sl += (int64_t)kSellRows * kSellWarps) {
       A acc[kSellRows];
-      sell_rows<S>(sptr, scol, sval, [&](int c) { return Tr::ld(y, c); }, sl, s_hi, acc);
+      sell_rows<S, CT>(sptr, scol, sval, [&](int c) { return Tr::ld(y, c); }, sl, s_hi, acc);
 #pragma unroll
       for (int u = 0; u < kSellRows; ++u) {
         if (!valid(sl, u)) continue;
@@ -268,13 +305,13 @@ pcg_sell_hs_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* _
         bb_l += b * b;
       }
     }
-    publish(pA, rz_l);
-    publish(pB, rr_l);
-    publish(pC, bb_l);
+    publish2(pA, rz_l, pB, rr_l);
+    const double t = block_sum(Tr::to_double(bb_l), s_red);
+    if (threadIdx.x == 0) pC[blockIdx.x] = t;
   }
   if (!grid_sync(st, nb, my_gen)) return;
-  double rz = sum_partials(pA, nb, s_red);
-  double rr = sum_partials(pB, nb, s_red);
+  double rz, rr;
+  sum_partials2(pA, pB, nb, s_red, rz, rr);
   const double bnorm = sqrt(sum_partials(pC, nb, s_red));
   const double tol = fmax(rtol * bnorm, atol);
   if (blockIdx.x == 0 && threadIdx.x == 0) st->bnorm = bnorm;
@@ -296,8 +333,8 @@ pcg_sell_hs_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* _
     const S* cpold = pold;
     for (int64_t sl = s_lo + warp; sl < s_hi; sl += (int64_t)kSellRows * kSellWarps) {
       A acc[kSellRows];
-      sell_rows<S>(sptr, scol, sval, [&](int c) { return Tr::ld(r, c) + beta * Tr::ld(cpold, c); }, sl, s_hi,
-                   acc);
+      sell_rows<S, CT>(sptr, scol, sval, [&](int c) { return Tr::ld(r, c) + beta * Tr::ld(cpold, c); }, sl,
+                       s_hi, acc);
 #pragma unroll
       for (int u = 0; u < kSellRows; ++u) {
         if (!valid(sl, u)) continue;
@@ -308,7 +345,10 @@ pcg_sell_hs_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* _
         pq_l += Tr::ld(dinv, row) * pv * acc[u];
       }
     }
-    publish(pA, pq_l);
+    {
+      const double t = block_sum(Tr::to_double(pq_l), s_red);
+      if (threadIdx.x == 0) pA[blockIdx.x] = t;
+    }
     if (!grid_sync(st, nb, my_gen)) return;
     const double pq = sum_partials(pA, nb, s_red);
     if (!(pq > 0.0)) {
@@ -329,11 +369,10 @@ pcg_sell_hs_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* _
       rz_l += di * rn * rn;
       rr_l += rn * rn;
     }
-    publish(pB, rz_l);
-    publish(pC, rr_l);
+    publish2(pB, rz_l, pC, rr_l);
     if (!grid_sync(st, nb, my_gen)) return;
-    const double rzn = sum_partials(pB, nb, s_red);
-    rr = sum_partials(pC, nb, s_red);
+    double rzn;
+    sum_partials2(pB, pC, nb, s_red, rzn, rr);
     beta = Tr::from_double(rzn / rz);
     rz = rzn;
     S* t = pold;
@@ -351,9 +390,9 @@ pcg_sell_hs_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* _
   }
 }
 
-template <class S>
+template <class S, class CT>
 __global__ void __launch_bounds__(kSellThreads, 2)
-pcg_sell_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __restrict__ scol,
+pcg_sell_kernel(int64_t n, const int64_t* __restrict__ sptr, const CT* __restrict__ scol,
                 const S* __restrict__ sval, const S* __restrict__ dinv, const typename SellT<S>::V* __restrict__ bv,
                 typename SellT<S>::V* __restrict__ xv, S* x, S* r, S* p, S* s, S* z, S* w0, S* w1,
                 double* partials, PcgState* st, double rtol, double atol, int maxiter) {
@@ -384,7 +423,7 @@ pcg_sell_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __re
   A bb_l = Tr::zero();
   for (int64_t sl = s_lo + warp; sl < s_hi; sl += (int64_t)kSellRows * kSellWarps) {
     A acc[kSellRows];
-    sell_rows<S>(sptr, scol, sval, [&](int c) { return Tr::ld(z, c); }, sl, s_hi, acc);
+    sell_rows<S, CT>(sptr, scol, sval, [&](int c) { return Tr::ld(z, c); }, sl, s_hi, acc);
 #pragma unroll
     for (int u = 0; u < kSellRows; ++u) {
       if (!valid(sl, u)) continue;
@@ -412,7 +451,7 @@ pcg_sell_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __re
     A g_l = Tr::zero(), d_l = Tr::zero(), r_l = Tr::zero();
     for (int64_t sl = s_lo + warp; sl < s_hi; sl += (int64_t)kSellRows * kSellWarps) {
       A acc[kSellRows];
-      sell_rows<S>(sptr, scol, sval, [&](int c) { return Tr::ld(r, c); }, sl, s_hi, acc);
+      sell_rows<S, CT>(sptr, scol, sval, [&](int c) { return Tr::ld(r, c); }, sl, s_hi, acc);
 #pragma unroll
       for (int u = 0; u < kSellRows; ++u) {
         if (!valid(sl, u)) continue;
@@ -456,7 +495,7 @@ pcg_sell_kernel(int64_t n, const int64_t* __restrict__ sptr, const int32_t* __re
     A g_l = Tr::zero(), d_l = Tr::zero(), r_l = Tr::zero();
     for (int64_t sl = s_lo + warp; sl < s_hi; sl += (int64_t)kSellRows * kSellWarps) {
       A acc[kSellRows];
-      sell_rows<S>(sptr, scol, sval, [&](int c) { return Tr::ld(wc, c); }, sl, s_hi, acc);
+      sell_rows<S, CT>(sptr, scol, sval, [&](int c) { return Tr::ld(wc, c); }, sl, s_hi, acc);
 #pragma unroll
       for (int u = 0; u < kSellRows; ++u) {
         if (!valid(sl, u)) continue;
@@ -509,12 +548,11 @@ int sell_blocks(K kern) {
   return min(kSellMaxBlocks, sms * min(per_sm, 2));
 }
 
-template <class S>
+template <class S, class CT>
 int launch_pcg_sell(int64_t n, const int64_t* indptr, const int32_t* indices, const typename SellT<S>::V* values,
                     const int64_t* sptr, int64_t n_pad, const typename SellT<S>::V* b, typename SellT<S>::V* x,
-                    double rtol, double atol, int maxiter, int method, char* w, cudaStream_t s) {
-  const bool pipe = method == TM_PCG_PIPELINED;
-  const int nb = pipe ? sell_blocks(pcg_sell_kernel<S>) : sell_blocks(pcg_sell_hs_kernel<S>);
+                    double rtol, double atol, int maxiter, bool pipe, char* w, cudaStream_t s) {
+  const int nb = pipe ? sell_blocks(pcg_sell_kernel<S, CT>) : sell_blocks(pcg_sell_hs_kernel<S, CT>);
   if (nb <= 0) return TM_ERR_CUDA;
   PcgState* st = reinterpret_cast<PcgState*>(w);
   char* q = w + 256;
@@ -527,16 +565,16 @@ int launch_pcg_sell(int64_t n, const int64_t* indptr, const int32_t* indices, co
   }
   S* sval = reinterpret_cast<S*>(q);
   q += align256(n_pad * (int64_t)sizeof(S));
-  int32_t* scol = reinterpret_cast<int32_t*>(q);
+  CT* scol = reinterpret_cast<CT*>(q);
   S* dinv = vec[0];
   S* y = vec[5];  // M^-1 x0, read by the first sweep only
   if (cudaMemsetAsync(st, 0, sizeof(PcgState), s) != cudaSuccess) return TM_ERR_CUDA;
   sell_dinv_kernel<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, indptr, indices, values, dinv);
   const int64_t n_slices = (n + 31) >> 5;
-  sell_fill_kernel<S><<<(unsigned)((n_slices * 32 + 255) / 256), 256, 0, s>>>(n, indptr, indices, values, sptr, n_pad,
-                                                                              dinv, x, scol, sval, y, st);
+  sell_fill_kernel<S, CT><<<(unsigned)((n_slices * 32 + 255) / 256), 256, 0, s>>>(n, indptr, indices, values, sptr,
+                                                                                  n_pad, dinv, x, scol, sval, y, st);
   if (cudaPeekAtLastError() != cudaSuccess) return TM_ERR_CUDA;
-  const int32_t* cscol = scol;
+  const CT* cscol = scol;
   const S* csval = sval;
   const S* cdinv = dinv;
   cudaError_t e;
@@ -545,37 +583,57 @@ int launch_pcg_sell(int64_t n, const int64_t* indptr, const int32_t* indices, co
     void* args[] = {(void*)&n, (void*)&sptr, (void*)&cscol, (void*)&csval, (void*)&cdinv, (void*)&b, (void*)&x,
                     (void*)&xs, (void*)&r, (void*)&p, (void*)&sv, (void*)&z, (void*)&w0, (void*)&w1,
                     (void*)&partials, (void*)&st, (void*)&rtol, (void*)&atol, (void*)&maxiter};
-    e = cudaLaunchCooperativeKernel((const void*)pcg_sell_kernel<S>, dim3(nb), dim3(kSellThreads), args, 0, s);
+    e = cudaLaunchCooperativeKernel((const void*)pcg_sell_kernel<S, CT>, dim3(nb), dim3(kSellThreads), args, 0, s);
   } else {
     S *xs = vec[1], *r = vec[2], *qv = vec[3], *pt0 = vec[4], *pt1 = vec[6];
     const S* cy = y;
     void* args[] = {(void*)&n, (void*)&sptr, (void*)&cscol, (void*)&csval, (void*)&cdinv, (void*)&b, (void*)&x,
                     (void*)&xs, (void*)&r, (void*)&qv, (void*)&pt0, (void*)&pt1, (void*)&cy,
                     (void*)&partials, (void*)&st, (void*)&rtol, (void*)&atol, (void*)&maxiter};
-    e = cudaLaunchCooperativeKernel((const void*)pcg_sell_hs_kernel<S>, dim3(nb), dim3(kSellThreads), args, 0, s);
+    e = cudaLaunchCooperativeKernel((const void*)pcg_sell_hs_kernel<S, CT>, dim3(nb), dim3(kSellThreads), args, 0,
+                                    s);
   }
   return e == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
 
+template <class S>
+int launch_pcg_sell_any(int64_t n, const int64_t* indptr, const int32_t* indices, const typename SellT<S>::V* values,
+                        const int64_t* sptr, int64_t n_pad, const typename SellT<S>::V* b, typename SellT<S>::V* x,
+                        double rtol, double atol, int maxiter, int method, char* w, cudaStream_t s) {
+  const bool pipe = (method & 1) == TM_PCG_PIPELINED;
+  if (method & TM_PCG_NARROW)
+    return launch_pcg_sell<S, int16_t>(n, indptr, indices, values, sptr, n_pad, b, x, rtol, atol, maxiter, pipe, w, s);
+  return launch_pcg_sell<S, int32_t>(n, indptr, indices, values, sptr, n_pad, b, x, rtol, atol, maxiter, pipe, w, s);
+}
+
 }  // namespace tmg
 
-extern "C" int64_t tm_sell_plan(int64_t n, const int64_t* indptr, int64_t* slice_ptr, void* stream) {
+extern "C" int64_t tm_sell_plan(int64_t n, const int64_t* indptr, const int32_t* indices, int64_t* slice_ptr,
+                                int32_t* out_narrow, void* stream) {
   if (n < 0) return -TM_ERR_INVALID;
-  if (!slice_ptr || (n > 0 && !indptr)) return -TM_ERR_INVALID;
+  if (!slice_ptr || (n > 0 && (!indptr || !indices))) return -TM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int64_t n_slices = (n + 31) >> 5;
+  if (out_narrow) *out_narrow = 1;
   if (n_slices == 0) {
     const int64_t zero = 0;
     if (cudaMemcpyAsync(slice_ptr, &zero, sizeof(zero), cudaMemcpyHostToDevice, s) != cudaSuccess) return -TM_ERR_CUDA;
     return cudaStreamSynchronize(s) == cudaSuccess ? 0 : -TM_ERR_CUDA;
   }
+  // slice_ptr[0] first collects the largest |column - row| (the scan then sets it to 0)
+  if (cudaMemsetAsync(slice_ptr, 0, sizeof(int64_t), s) != cudaSuccess) return -TM_ERR_CUDA;
   tmg::sell_width_kernel<<<(unsigned)((n_slices * 32 + 255) / 256), 256, 0, s>>>(n, indptr, slice_ptr);
+  tmg::sell_span_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, indptr, indices,
+                                                                   reinterpret_cast<unsigned long long*>(slice_ptr));
+  int64_t span = 0;
+  if (cudaMemcpyAsync(&span, slice_ptr, sizeof(span), cudaMemcpyDeviceToHost, s) != cudaSuccess) return -TM_ERR_CUDA;
   tmg::sell_scan_kernel<<<1, 1024, 0, s>>>(n_slices, slice_ptr);
   if (cudaPeekAtLastError() != cudaSuccess) return -TM_ERR_CUDA;
   int64_t total = 0;
   if (cudaMemcpyAsync(&total, slice_ptr + n_slices, sizeof(total), cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return -TM_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return -TM_ERR_CUDA;
+  if (out_narrow) *out_narrow = span <= 32767 ? 1 : 0;
   if (total >= (int64_t(1) << 40)) return -TM_ERR_INDEX;
   return total;
 }
@@ -592,7 +650,7 @@ extern "C" int tm_pcg_jacobi_sell(int32_t dtype, int64_t n, const int64_t* indpt
                                   double rtol, double atol, int32_t maxiter, int32_t method, void* work,
                                   int64_t work_bytes, void* stream) {
   if (n < 0 || n_pad < 0 || maxiter < 0) return TM_ERR_INVALID;
-  if (method != TM_PCG_STANDARD && method != TM_PCG_PIPELINED) return TM_ERR_INVALID;
+  if (method < 0 || method > (TM_PCG_PIPELINED | TM_PCG_NARROW)) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   if (!indptr || !indices || !values || !slice_ptr || !b || !x || !work) return TM_ERR_INVALID;
   if (dtype != TM_F32 && dtype != TM_F64) return TM_ERR_INVALID;
@@ -601,8 +659,8 @@ extern "C" int tm_pcg_jacobi_sell(int32_t dtype, int64_t n, const int64_t* indpt
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   char* w = static_cast<char*>(work);
   if (dtype == TM_F64)
-    return tmg::launch_pcg_sell<tmg::F2>(n, indptr, indices, (const double*)values, slice_ptr, n_pad,
+    return tmg::launch_pcg_sell_any<tmg::F2>(n, indptr, indices, (const double*)values, slice_ptr, n_pad,
                                          (const double*)b, (double*)x, rtol, atol, maxiter, method, w, s);
-  return tmg::launch_pcg_sell<float>(n, indptr, indices, (const float*)values, slice_ptr, n_pad, (const float*)b,
+  return tmg::launch_pcg_sell_any<float>(n, indptr, indices, (const float*)values, slice_ptr, n_pad, (const float*)b,
                                      (float*)x, rtol, atol, maxiter, method, w, s);
 }

@@ -148,19 +148,23 @@ def workspace(n, nnz, dtype, device) -> PCGWorkspace:
     return _cached(("csr", n, nnz, dtype, str(device)), lambda: PCGWorkspace(n, nnz, dtype, device))
 
 
-def sell_plan(indptr: torch.Tensor):
-    """(slice_ptr, n_pad) of the SELL-32 layout of a CSR pattern (tm_sell_plan),
-    cached on the indptr tensor while it is unmodified."""
-    cached = getattr(indptr, "_tm_sell", None)
-    if cached is not None and cached[0] == indptr._version:
-        return cached[1], cached[2]
+def sell_plan(indptr: torch.Tensor, indices: torch.Tensor):
+    """(slice_ptr, n_pad, narrow) of the SELL-32 layout of a CSR pattern
+    (tm_sell_plan; narrow: every |column - row| fits 16 bits), cached on the
+    indices tensor while the pattern tensors are unmodified."""
+    key = (indptr.data_ptr(), indptr._version, indices._version)
+    cached = getattr(indices, "_tm_sell", None)
+    if cached is not None and cached[0] == key:
+        return cached[1], cached[2], cached[3]
     n = indptr.shape[0] - 1
     sp = torch.empty((n + 31) // 32 + 1, dtype=torch.int64, device=indptr.device)
-    n_pad = int(_lib.load().tm_sell_plan(n, indptr.data_ptr(), sp.data_ptr(), _lib.stream_handle(indptr.device)))
+    narrow = _lib.ctypes.c_int32(0)
+    n_pad = int(_lib.load().tm_sell_plan(n, indptr.data_ptr(), indices.data_ptr(), sp.data_ptr(),
+                                         _lib.ctypes.byref(narrow), _lib.stream_handle(indptr.device)))
     if n_pad < 0:
         raise _lib.TensorMeshCudaError("tm_sell_plan", -n_pad)
-    indptr._tm_sell = (indptr._version, sp, n_pad)
-    return sp, n_pad
+    indices._tm_sell = (key, sp, n_pad, bool(narrow.value))
+    return sp, n_pad, bool(narrow.value)
 
 
 # "sell": standard PCG over the SELL-32 copy (tm_pcg_jacobi_sell); "sell-pipelined":
@@ -185,9 +189,9 @@ def pcg_jacobi_raw(indptr, indices, values, b, x, rtol=1e-8, atol=0.0, maxiter=1
     code = _dt(values)
     pipelined = LAYOUT == "sell-pipelined"
     if LAYOUT in ("sell", "sell-pipelined"):
-        sp, n_pad = sell_plan(indptr)
+        sp, n_pad, narrow = sell_plan(indptr, indices)
         ws = _cached(("sell", n, n_pad, values.dtype, str(dev)), lambda: SellWorkspace(n, n_pad, values.dtype, dev))
-        method = _lib.TM_PCG_PIPELINED if pipelined else _lib.TM_PCG_STANDARD
+        method = (_lib.TM_PCG_PIPELINED if pipelined else _lib.TM_PCG_STANDARD) | (_lib.TM_PCG_NARROW if narrow else 0)
 
         def launch(rhs, sol, rt, at, budget):
             _lib.call("tm_pcg_jacobi_sell", code, n, indptr.data_ptr(), indices.data_ptr(), values.data_ptr(),

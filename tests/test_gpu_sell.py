@@ -62,12 +62,12 @@ def slice_plan_reference(indptr, n):
 def test_sell_plan_and_solve_on_ragged_matrices(n):
     ip, ix, dv = random_spd(n, seed=n)
     indptr = torch.from_numpy(ip).to(DEV)
-    sp, n_pad = S.sell_plan(indptr)
+    indices = torch.from_numpy(ix).to(DEV)
+    sp, n_pad, narrow = S.sell_plan(indptr, indices)
     ref = slice_plan_reference(ip, n)
     np.testing.assert_array_equal(sp.cpu().numpy(), ref)
-    assert n_pad == int(ref[-1])
+    assert n_pad == int(ref[-1]) and narrow
     b = np.random.default_rng(n + 1).normal(size=n)
-    indices = torch.from_numpy(ix).to(DEV)
     values = torch.from_numpy(dv).to(DEV)
     x = torch.zeros(n, dtype=torch.float64, device=DEV)
     info = S.pcg_jacobi_raw(indptr, indices, values, torch.from_numpy(b).to(DEV), x, rtol=1e-12)
@@ -101,7 +101,7 @@ def test_sell_nonzero_initial_guess_and_iteration_cap():
     x = x0.clone()
     info = S.pcg_jacobi_raw(K_ii.indptr, K_ii.indices, K_ii.values, f_i, x, rtol=1e-11)
     assert info.status == 0 and info.residual <= 1e-11
-    sp, n_pad = S.sell_plan(K_ii.indptr)
+    sp, n_pad, _ = S.sell_plan(K_ii.indptr, K_ii.indices)
     n = f_i.shape[0]
     ws = S.SellWorkspace(n, n_pad, torch.float64, f_i.device)
     x = torch.zeros_like(f_i)
@@ -125,7 +125,7 @@ def test_sell_plan_of_another_pattern_is_rejected():
     through the solver record; the kernel writes and iterates nothing."""
     K_ii, f_i = poisson(8)
     n = f_i.shape[0]
-    sp, n_pad = S.sell_plan(K_ii.indptr)
+    sp, n_pad, _ = S.sell_plan(K_ii.indptr, K_ii.indices)
     bad = sp.clone()
     bad[1:] = bad[1:] // 2 // 32 * 32       # half the widths: rows no longer fit
     bad[-1] = n_pad
@@ -148,7 +148,7 @@ def test_sell_plan_of_another_pattern_is_rejected():
                                   1e-8, 0.0, 100, 0, ws.buf.data_ptr(), ws.nbytes, s) == _lib.TM_ERR_INVALID
     assert lib.tm_pcg_jacobi_sell(_lib.TM_F64, n, K_ii.indptr.data_ptr(), K_ii.indices.data_ptr(),
                                   K_ii.values.data_ptr(), sp.data_ptr(), n_pad, f_i.data_ptr(), x.data_ptr(),
-                                  1e-8, 0.0, 100, 2, ws.buf.data_ptr(), ws.nbytes, s) == _lib.TM_ERR_INVALID
+                                  1e-8, 0.0, 100, 4, ws.buf.data_ptr(), ws.nbytes, s) == _lib.TM_ERR_INVALID
 
 
 def test_sell_solve_is_bitwise_repeatable():
@@ -173,3 +173,40 @@ def test_pipelined_form_converges_in_double_float(monkeypatch):
     xr = torch.zeros_like(f_i)
     S.pcg_jacobi_raw(K_ii.indptr, K_ii.indices, K_ii.values, f_i, xr, rtol=1e-10)
     assert float((x - xr).abs().max() / xr.abs().max()) <= 1e-7
+
+
+def test_wide_couplings_keep_32_bit_columns(monkeypatch):
+    """A coupling farther than 32767 rows from the diagonal: the plan reports
+    the pattern as wide, the solve takes 32-bit columns and converges; a
+    caller that claims 16-bit columns anyway gets TM_ERR_INDEX."""
+    n = 40000
+    rows = np.arange(n)
+    ip = np.zeros(n + 1, np.int64)
+    cols, vals = [], []
+    for i in range(n):           # tridiagonal, plus a coupling of rows 0 and n - 1
+        row_c = [c for c in (i - 1, i, i + 1) if 0 <= c < n]
+        if i == 0:
+            row_c.append(n - 1)
+        if i == n - 1:
+            row_c.insert(0, 0)
+        cols.extend(row_c)
+        vals.extend([4.0 if c == i else -1.0 for c in row_c])
+        ip[i + 1] = len(cols)
+    indptr = torch.from_numpy(ip).to(DEV)
+    indices = torch.tensor(cols, dtype=torch.int32, device=DEV)
+    values = torch.tensor(vals, dtype=torch.float64, device=DEV)
+    sp, n_pad, narrow = S.sell_plan(indptr, indices)
+    assert not narrow
+    b = torch.ones(n, dtype=torch.float64, device=DEV)
+    x = torch.zeros_like(b)
+    info = S.pcg_jacobi_raw(indptr, indices, values, b, x, rtol=1e-10)
+    assert info.status == 0 and info.residual <= 1e-10
+    ws = S.SellWorkspace(n, n_pad, torch.float64, b.device)
+    lib = _lib.load()
+    s = _lib.stream_handle(b.device)
+    x = torch.zeros_like(b)
+    assert lib.tm_pcg_jacobi_sell(_lib.TM_F64, n, indptr.data_ptr(), indices.data_ptr(), values.data_ptr(),
+                                  sp.data_ptr(), n_pad, b.data_ptr(), x.data_ptr(), 1e-8, 0.0, 100,
+                                  _lib.TM_PCG_NARROW, ws.buf.data_ptr(), ws.nbytes, s) == 0
+    assert lib.tm_pcg_result(ws.buf.data_ptr(), None, None, None, s) == _lib.TM_ERR_INDEX
+    assert int(torch.count_nonzero(x)) == 0
