@@ -528,10 +528,40 @@ def run_ours(args):
         tb = time.perf_counter()
         info = K_ii.last_solve_info
         it_bytes = 12 * K_ii.nnz + 4 * (K_ii.shape[0] + 1) + 80 * K_ii.shape[0]
+        from tensormesh_gb300 import solve as solve_mod
+        _, n_pad, narrow = solve_mod.sell_plan(K_ii.indptr, K_ii.indices)
+        ach = it_bytes * info.iterations / (tb - ta) / 1e9
         pcg = {"jacobi_seconds_to_1e-8": tb - ta, "iterations": info.iterations, "true_residual": info.residual,
                "status": info.status, "n": K_ii.shape[0], "nnz": K_ii.nnz,
-               "per_iteration_algorithmic_bytes": it_bytes,
-               "achieved_gbs": it_bytes * info.iterations / (tb - ta) / 1e9, "learned_seconds_to_1e-8": None}
+               "kernel": "tm_pcg_jacobi_sell, standard form, SELL-32 copy (%d padded entries, %s-bit columns)"
+                         % (n_pad, "16" if narrow else "32"),
+               "per_iteration_algorithmic_bytes": it_bytes, "ms_per_iteration": 1e3 * (tb - ta) / max(1, info.iterations),
+               "achieved_gbs": ach,
+               "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                            "peak_source": peak_src,
+                            "note": "whole solve (plan cached, SELL fill, iterations, FP64 true-residual check) "
+                                    "over iterations x the algorithmic bytes of one iteration"},
+               "learned_seconds_to_1e-8": None}
+        if rank == 0 and world == 1 and not args.no_cpu:
+            # the reference's Jacobi-PCG operation sequence on the host cores,
+            # timed on a bounded number of iterations of the same system
+            from oracle.torch_ref import ReferenceJacobiPCG
+            threads = os.cpu_count() or 1
+            torch.set_num_threads(threads)
+            ref = ReferenceJacobiPCG(K_ii.indptr.cpu().numpy(), K_ii.indices.cpu().numpy(),
+                                     K_ii.values.cpu().numpy())
+            bh = f_i.cpu()
+            ref.iterate(bh, 2)
+            n_it = 20
+            t0c = time.perf_counter()
+            ref.iterate(bh, n_it)
+            sec_it = (time.perf_counter() - t0c) / n_it
+            pcg["cpu_baseline"] = {"seconds_per_iteration": sec_it, "cores": threads, "kind": "reference-torch",
+                                   "projected_seconds_to_1e-8": sec_it * info.iterations,
+                                   "sample": f"{n_it} iterations of the reference's CG loop with its Jacobi "
+                                             "preconditioner (torch CSR on the host, oracle/torch_ref.py), "
+                                             "projected to the GPU solve's iteration count"}
+            del ref
         wpath = os.path.join(ROOT, "tensormesh_gb300", "weights", "mpnn_poisson_kuhn32.npz")
         if os.path.exists(wpath) and not args.no_learned:
             from tensormesh_gb300.learned import LearnedPreconditioner

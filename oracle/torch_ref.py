@@ -80,3 +80,44 @@ class ReferenceOps:
         out = out.index_add_(0, self.slots, Ke.reshape(-1))
         row, col = self.edges[0].long(), self.edges[1].long()            # noqa: F841
         return out
+
+
+class ReferenceJacobiPCG:
+    """The reference's iterative-solve operation sequence on the CPU: its CG
+    loop (``cg_py``, sparse/solve/torch_solve.py:70-128: a torch CSR matrix,
+    one torch call per SpMV, dot and axpy) with its Jacobi preconditioner
+    applied the way ``jacobi_precond`` does it (torch_solve.py:24-59: the
+    diagonal with missing entries taken as 1, z = r * (1 / diag)).  The
+    reference's default ``K.solve`` backend (torch_sla) is not available, so
+    this stands for its Jacobi-PCG; it times iterations, it does not decide
+    convergence (the product's solver does that on the GPU)."""
+
+    def __init__(self, indptr: np.ndarray, indices: np.ndarray, values: np.ndarray):
+        n = indptr.shape[0] - 1
+        self.A = torch.sparse_csr_tensor(torch.from_numpy(indptr.astype(np.int64)),
+                                         torch.from_numpy(indices.astype(np.int64)),
+                                         torch.from_numpy(values), size=(n, n))
+        rows = np.repeat(np.arange(n), np.diff(indptr))
+        diag = np.ones(n)
+        on = rows == indices
+        diag[rows[on]] = values[on]
+        self.dinv = 1.0 / torch.from_numpy(diag)
+
+    def iterate(self, b: torch.Tensor, iters: int) -> torch.Tensor:
+        """``iters`` Jacobi-PCG iterations from x = 0; returns x."""
+        A, dinv = self.A, self.dinv
+        x = torch.zeros_like(b)
+        r = b - A @ x
+        z = r * dinv
+        p = z.clone()
+        rz = torch.dot(r, z)
+        for _ in range(iters):
+            Ap = A @ p
+            alpha = rz / torch.dot(p, Ap)
+            x = x + alpha * p
+            r = r - alpha * Ap
+            z = r * dinv
+            rz_new = torch.dot(r, z)
+            p = z + (rz_new / rz) * p
+            rz = rz_new
+        return x

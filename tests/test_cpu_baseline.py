@@ -107,3 +107,23 @@ def test_torch_reference_ops_time_like_the_reference():
     ratio = t_ops / t_ref
     print(f"reference __call__ {t_ref * 1e3:.1f} ms, torch restatement {t_ops * 1e3:.1f} ms, ratio {ratio:.2f}")
     assert 0.75 <= ratio <= 1.25, ratio
+
+
+def test_reference_jacobi_pcg_sequence_matches_the_oracle_solver():
+    """The timed CPU solve baseline (the reference's CG loop with its Jacobi
+    preconditioner, in torch) runs the oracle's Jacobi-PCG iteration."""
+    import warnings
+    import scipy.sparse as sp
+    from oracle import fem
+    from oracle.torch_ref import ReferenceJacobiPCG
+    n = 300
+    A = sp.random(n, n, density=0.03, random_state=3)
+    A = (A + A.T + 25.0 * sp.eye(n)).tocsr()
+    A.sort_indices()
+    b = np.random.default_rng(4).normal(size=n)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        ref = ReferenceJacobiPCG(A.indptr, A.indices, A.data)
+        x = ref.iterate(torch.from_numpy(b), 40).numpy()
+    xo, _, _ = fem.pcg_jacobi(A.indptr, A.indices.astype(np.int64), A.data, b, rtol=1e-14)
+    assert np.max(np.abs(x - xo)) <= 1e-10 * np.max(np.abs(xo))
