@@ -63,9 +63,10 @@ class MeshTopology:
         self._block = {}
         self._incidence = None
 
-    # accumulator budget per patch in node slots: ~100 KB of shared memory at
-    # 8 bytes per value, divided by the H*H values of a block slot
-    _SLOT_BUDGET = {1: 6144, 2: 1600, 3: 700}
+    # accumulator budget per patch in node slots (the scalar forms' kernels
+    # autotune it; 3x3 blocks: 512 slots = 36 KB of accumulators, so three
+    # elasticity CTAs fit an SM)
+    _SLOT_BUDGET = {1: 6144, 2: 1600, 3: 512}
 
     def plan_for(self, H: int, budget: int = None):
         """(PatchPlan, ctypes struct) sized for H x H block slots (or for an
