@@ -74,16 +74,9 @@ __device__ __forceinline__ bool p1tet_elast_pass(const tm_patch_plan& plan, cons
 #pragma unroll
       for (int j = 0; j < 3; ++j) s_acc[((ro + k) * 3 + comp) * 3 + j] = P::st(P::zero());
   }
-  const T* pts = static_cast<const T*>(args.points);
-  const FrameInfo fr = patch_frame<3, T>(pts, plan.vtx + vbeg, nv, s_R, s_red);
-  if (fr.bad && kGuard) return false;  // a non-finite coordinate: the native pass writes nan
-  bool flag = kGuard && args.coef_kind == TM_COEF_SCALAR && !coef_in_range(args.scal[0]);
+  // the first chunk's element data does not depend on the frame: its loads
+  // are issued first, in flight while the frame's gathers and reductions run
   const T* coef = static_cast<const T*>(args.coef);
-  double wsum = 0.0;
-  for (int q = 0; q < Q; ++q) wsum += args.tables[q];
-  const A W = P::in(wsum);
-  const A sc = P::in(args.scal[0]);
-  const A lam1 = P::in(args.lam), mu1 = P::in(args.mu);
   const bool per_elem = args.coef_kind == TM_COEF_ELEMENT;
   const bool worker = tid < chunk;
   uint2 cw_next = make_uint2(0u, 0u);
@@ -92,6 +85,15 @@ __device__ __forceinline__ bool p1tet_elast_pass(const tm_patch_plan& plan, cons
     cw_next = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)(ebeg + tid) * 4);
     if (per_elem) c_next = coef[plan.elem[ebeg + tid]];
   }
+  const T* pts = static_cast<const T*>(args.points);
+  const FrameInfo fr = patch_frame<3, T>(pts, plan.vtx + vbeg, nv, s_R, s_red);
+  if (fr.bad && kGuard) return false;  // a non-finite coordinate: the native pass writes nan
+  bool flag = kGuard && args.coef_kind == TM_COEF_SCALAR && !coef_in_range(args.scal[0]);
+  double wsum = 0.0;
+  for (int q = 0; q < Q; ++q) wsum += args.tables[q];
+  const A W = P::in(wsum);
+  const A sc = P::in(args.scal[0]);
+  const A lam1 = P::in(args.lam), mu1 = P::in(args.mu);
   __syncthreads();
 
   for (int cbeg = 0; cbeg < ne; cbeg += chunk) {

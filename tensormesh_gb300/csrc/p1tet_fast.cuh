@@ -225,7 +225,26 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
   S* s_acc = reinterpret_cast<S*>(sm.acc);
   S* s_stage = reinterpret_cast<S*>(sm.stage);
 
-  // ---- phase 0: frame, point coefficients, zeroed accumulators, cursors
+  // ---- phase 0: frame, point coefficients, zeroed accumulators, cursors.
+  // The first chunk's element data and each owner's first record do not
+  // depend on the frame: their loads are issued first, so that they are in
+  // flight while the frame's coordinate gathers and reductions run.
+  const T* coef = static_cast<const T*>(args.coef);
+  const bool per_elem = args.coef_kind == TM_COEF_ELEMENT;
+  // element data of this thread's next element (thread tid handles element
+  // c * kTetChunk + tid of chunk c), loaded one chunk ahead
+  uint2 cw_next = make_uint2(0u, 0u);
+  T c_next = T(0);
+  if (tid < ne) {
+    cw_next = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)(ebeg + tid) * 4);
+    if (per_elem) c_next = coef[plan.elem[ebeg + tid]];
+  }
+  int cur = 0;
+  RW rec = R::kEnd;
+  if (row.owner) {
+    cur = row.cur0;
+    if (cur < row.end) rec = recs[cur];
+  }
   const T* pts = static_cast<const T*>(args.points);
   const FrameInfo fr = patch_frame<3, T>(pts, plan.vtx + vbeg, nv, sm.R, sm.red);
   if (fr.bad) {
@@ -241,31 +260,16 @@ __device__ __forceinline__ bool p1tet_laplace_pass(const tm_patch_plan& plan, co
   const int kf = fr.k;
   const ShortConv sconv = short_conv(fr.t + fr.z - 62);
   const double esc_native = std::is_same<A, double>::value ? ldexp(1.0, fr.z - 62) : 0.0;
-  const T* coef = static_cast<const T*>(args.coef);
   if (args.coef_kind == TM_COEF_POINT)
     for (int i = tid; i < nv; i += kThreads) s_pc[i] = P::st(P::in(coef[plan.vtx[vbeg + i]]));
   S* acc = s_acc + tid;  // this thread's row: entry k at acc[k * nrp]
-  int cur = 0;
-  RW rec = R::kEnd;
-  if (row.owner) {
+  if (row.owner)
     for (int k = 0; k < row.deg; ++k) acc[k * nrp] = P::st(P::zero());
-    cur = row.cur0;
-    if (cur < row.end) rec = recs[cur];
-  }
   double wsum = 0.0;
   for (int q = 0; q < Q; ++q) wsum += args.tables[q];
   const A W = P::in(wsum);
   const double sc_raw = args.scal[0];
   const A sc = P::in(sc_raw);
-  const bool per_elem = args.coef_kind == TM_COEF_ELEMENT;
-  // element data of this thread's next element (thread tid handles element
-  // c * kTetChunk + tid of chunk c), loaded one chunk ahead
-  uint2 cw_next = make_uint2(0u, 0u);
-  T c_next = T(0);
-  if (tid < ne) {
-    cw_next = *reinterpret_cast<const uint2*>(plan.econn + (int64_t)(ebeg + tid) * 4);
-    if (per_elem) c_next = coef[plan.elem[ebeg + tid]];
-  }
   bool flag = kGuard && !coef_in_range((double)sc_raw) && args.coef_kind == TM_COEF_SCALAR;
   __syncthreads();
 

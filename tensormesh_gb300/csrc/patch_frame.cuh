@@ -157,11 +157,21 @@ TM_D FrameInfo patch_frame(const T* __restrict__ pts, const int32_t* __restrict_
   FrameInfo fi{0, 0, 0, false, false};
   if (tid < 3) s_red[tid] = 0ull;
   __syncthreads();
-  // pass 1: the largest biased exponent of the patch's coordinates
+  // pass 1: the largest biased exponent of the patch's coordinates (four
+  // index loads, then four coordinate loads, in flight per round)
   int emax = 1;
-  for (int i = tid; i < nv * D; i += nth) {
-    const T x = pts[(int64_t)vtx[i / D] * D + i % D];
-    emax = max(emax, tm_bexp(x));
+  for (int i0 = tid; i0 < nv * D; i0 += 4 * nth) {
+    int64_t at[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * nth;
+      at[u] = i < nv * D ? (int64_t)vtx[i / D] * D + i % D : -1;
+    }
+    T x[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) x[u] = at[u] >= 0 ? pts[at[u]] : T(0);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) emax = max(emax, tm_bexp(x[u]));
   }
   if (emax > 1) atomicMax(reinterpret_cast<unsigned long long*>(s_red), (unsigned long long)emax);
   __syncthreads();
@@ -175,12 +185,26 @@ TM_D FrameInfo patch_frame(const T* __restrict__ pts, const int32_t* __restrict_
 #pragma unroll
   for (int d = 0; d < D; ++d) O[d] = tm_fixed(pts[v0 * D + d], Ep);
   unsigned long long amax = 0ull, bits = 0ull;
-  for (int i = tid; i < nv * D; i += nth) {
-    const long long r = tm_fixed(pts[(int64_t)vtx[i / D] * D + i % D], Ep) - O[i % D];
-    s_R[i] = r;
-    const unsigned long long a = (unsigned long long)(r < 0 ? -r : r);
-    amax = a > amax ? a : amax;
-    bits |= a;
+  for (int i0 = tid; i0 < nv * D; i0 += 4 * nth) {
+    int64_t at[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * nth;
+      at[u] = i < nv * D ? (int64_t)vtx[i / D] * D + i % D : -1;
+    }
+    T x[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) x[u] = at[u] >= 0 ? pts[at[u]] : T(0);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * nth;
+      if (i >= nv * D) break;
+      const long long r = tm_fixed(x[u], Ep) - O[i % D];
+      s_R[i] = r;
+      const unsigned long long a = (unsigned long long)(r < 0 ? -r : r);
+      amax = a > amax ? a : amax;
+      bits |= a;
+    }
   }
   if (amax) atomicMax(s_red + 1, amax);
   if (bits) atomicOr(s_red + 2, bits);
