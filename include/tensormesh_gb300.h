@@ -262,6 +262,32 @@ typedef struct tm_twolevel {
 int tm_twolevel_apply(const tm_twolevel* t, const double* r, double* z, void* stream);
 
 /*
+ * `iters` iterations of flexible CG (Polak-Ribiere beta, clamped at 0) with
+ * the two-level preconditioner, on FP64 vectors, with every scalar on the
+ * device (graph-capturable, no host synchronisation):
+ *   q = A p; alpha = rz / (p, q); x += alpha p; r -= alpha q; z = M r;
+ *   beta = max(0, -alpha (z, q) / rz); rz = (r, z); p = z + beta p.
+ * A is the FP64 CSR matrix (a_*), M the two-level operator t.  x, r, p are
+ * updated in place; q and z are scratch of n doubles; sc[0] holds rz on
+ * entry and on exit (sc: 8 doubles: rz, alpha, beta, (p, q)); part is
+ * scratch of tm_fcg_workspace_doubles() doubles.  Dot products reduce in a
+ * fixed order (bitwise repeatable).  A non-positive (p, q) sets alpha = 0.
+ */
+int64_t tm_fcg_workspace_doubles(void);
+/* K P of the two-level coarse space (P piecewise constant over aggregates
+ * agg[n]): tm_kp_count writes count[i], the aggregates among the columns of
+ * row i; kp_indptr is its exclusive scan; tm_kp_fill writes row i as
+ * (aggregate, sum of K_ij over its columns j in CSR order) in ascending
+ * aggregate order.  FP64 values. */
+int tm_kp_count(int64_t n, const int64_t* indptr, const int32_t* indices, const int32_t* agg, int64_t* count,
+                void* stream);
+int tm_kp_fill(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values, const int32_t* agg,
+               const int64_t* kp_indptr, int32_t* kp_indices, double* kp_values, void* stream);
+int tm_fcg_twolevel_iterations(const tm_twolevel* t, int64_t a_nnz, const int64_t* a_indptr, const int32_t* a_indices,
+                               const double* a_values, double* x, double* r, double* p, double* q, double* z,
+                               double* sc, double* part, int32_t iters, void* stream);
+
+/*
  * Neo-Hookean energy per element and its displacement gradient per (element,
  * local node) (replaces NeoHookeanModel.energy, assemble/builtin.py:220-334,
  * the quadrature loop of ElementAssembler.energy, element_assembler.py:

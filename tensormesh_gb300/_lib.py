@@ -40,6 +40,7 @@ EXPORTS = [
     "tm_pcg_jacobi_noalloc", "tm_twolevel_apply", "tm_neohookean", "tm_facet_load",
     "tm_selftest_barrier_timeout", "tm_pattern_workspace_bytes", "tm_pattern_count", "tm_pattern_fill",
     "tm_sell_plan", "tm_pcg_sell_workspace_bytes", "tm_pcg_jacobi_sell",
+    "tm_fcg_workspace_doubles", "tm_fcg_twolevel_iterations", "tm_kp_count", "tm_kp_fill",
 ]
 
 P = ctypes.c_void_p
@@ -136,6 +137,9 @@ def _declare(lib):
         "tm_pcg_jacobi_noalloc": [i64, P, P, P, P, P, ctypes.c_double, ctypes.c_double, i32,
                                   ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_double), P],
         "tm_twolevel_apply": [ctypes.POINTER(TwoLevel), P, P, P],
+        "tm_fcg_twolevel_iterations": [ctypes.POINTER(TwoLevel), i64, P, P, P, P, P, P, P, P, P, P, i32, P],
+        "tm_kp_count": [i64, P, P, P, P, P],
+        "tm_kp_fill": [i64, P, P, P, P, P, P, P, P],
         "tm_neohookean": [i32, i32, i32, P, P, P, i64, P, ctypes.c_double, ctypes.c_double, P, P, P],
         "tm_facet_load": [i32, i32, i32, P, P, P, P, i64, i32, P, ctypes.POINTER(ctypes.c_double), i32, P, P, P],
         "tm_selftest_barrier_timeout": [i32, i64, ctypes.POINTER(i32), P, P],
@@ -145,6 +149,8 @@ def _declare(lib):
                                P],
     }
     lib.tm_sell_plan.argtypes = [i64, P, P, P, ctypes.POINTER(i32), P]
+    lib.tm_fcg_workspace_doubles.argtypes = []
+    lib.tm_fcg_workspace_doubles.restype = i64
     lib.tm_sell_plan.restype = i64
     lib.tm_pcg_sell_workspace_bytes.argtypes = [i32, i64, i64]
     lib.tm_pcg_sell_workspace_bytes.restype = i64

@@ -59,18 +59,190 @@ __global__ void finish_kernel(int64_t n, const int32_t* __restrict__ agg, const 
   z[i] = (double)((yc[c] - yc2[c]) + s1[i]);
 }
 
+// ---- flexible CG with the two-level preconditioner, vector work fused ----
+// Scalars live on the device (no host round trip per iteration): sc[0] = rz
+// = (r, z), sc[1] = alpha, sc[2] = beta, sc[3] = (p, q).  Dot products
+// reduce per CTA (fixed tree) into part[], then one CTA sums part[] in a
+// fixed order, so every iteration is bitwise repeatable.
+constexpr int kFcgThreads = 512;
+constexpr int kFcgBlocks = 304;
+
+__device__ __forceinline__ double fcg_block_sum(double v, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;  // valid in thread 0
+}
+
+__device__ __forceinline__ double fcg_sum_parts(const double* part, int nb) {
+  // one warp, lane-strided then a shuffle tree: the same order every call
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nb; i += 32) v += part[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;  // valid in lane 0
+}
+
+// part[b] = this CTA's share of (a, b)
+__global__ void __launch_bounds__(kFcgThreads) fcg_dot_kernel(int64_t n, const double* __restrict__ a,
+                                                               const double* __restrict__ b, double* part) {
+  __shared__ double red[32];
+  double v = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v = fma(a[i], b[i], v);
+  v = fcg_block_sum(v, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = v;
+}
+
+// alpha = rz / (p, q) (0 when (p, q) <= 0: the iteration then stands still
+// and the host's stagnation test takes over)
+__global__ void fcg_alpha_kernel(const double* part, int nb, double* sc) {
+  const double pq = fcg_sum_parts(part, nb);
+  if (threadIdx.x == 0) {
+    sc[3] = pq;
+    sc[1] = pq > 0.0 ? sc[0] / pq : 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(kFcgThreads) fcg_xr_kernel(int64_t n, double* __restrict__ x,
+                                                              double* __restrict__ r, const double* __restrict__ p,
+                                                              const double* __restrict__ q, const double* sc) {
+  const double alpha = sc[1];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = fma(alpha, p[i], x[i]);
+    r[i] = fma(-alpha, q[i], r[i]);
+  }
+}
+
+// part[b] = share of (r, z), part[nb + b] = share of (z, q)
+__global__ void __launch_bounds__(kFcgThreads) fcg_dot2_kernel(int64_t n, const double* __restrict__ r,
+                                                                const double* __restrict__ z,
+                                                                const double* __restrict__ q, double* part) {
+  __shared__ double red[32];
+  double a = 0.0, c = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double zi = z[i];
+    a = fma(r[i], zi, a);
+    c = fma(zi, q[i], c);
+  }
+  a = fcg_block_sum(a, red);
+  c = fcg_block_sum(c, red);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = a;
+    part[gridDim.x + blockIdx.x] = c;
+  }
+}
+
+// Polak-Ribiere: beta = max(0, (z, r_new - r_old) / rz_old) with
+// r_new - r_old = -alpha q; then rz = (r_new, z)
+__global__ void fcg_beta_kernel(const double* part, int nb, double* sc) {
+  const double rzn = fcg_sum_parts(part, nb);
+  const double zq = fcg_sum_parts(part + nb, nb);
+  if (threadIdx.x == 0) {
+    const double rz = sc[0];
+    const double b = rz != 0.0 ? -sc[1] * zq / rz : 0.0;
+    sc[2] = b > 0.0 ? b : 0.0;
+    sc[0] = rzn;
+  }
+}
+
+__global__ void __launch_bounds__(kFcgThreads) fcg_p_kernel(int64_t n, double* __restrict__ p,
+                                                             const double* __restrict__ z, const double* sc) {
+  const double beta = sc[2];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = fma(beta, p[i], z[i]);
+}
+
+// ---- K P (the thin matrix of the coarse space) without a global sort -------
+// Row i of K P holds, for each aggregate c among the columns of row i of K,
+// the sum of K_ij over those columns j with agg[j] = c: columns in ascending
+// aggregate order, each sum taken in the row's CSR order.  One thread per row;
+// the aggregates are found by repeated minimum searches over the row (rows
+// are short), so no per-row storage is needed.
+__global__ void kp_count_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ idx,
+                                const int32_t* __restrict__ agg, int64_t* __restrict__ count) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t k0 = indptr[i], k1 = indptr[i + 1];
+  int64_t m = 0;
+  int cur = -1;
+  for (;;) {
+    int nxt = 0x7fffffff;
+    for (int64_t k = k0; k < k1; ++k) {
+      const int a = agg[idx[k]];
+      if (a > cur && a < nxt) nxt = a;
+    }
+    if (nxt == 0x7fffffff) break;
+    ++m;
+    cur = nxt;
+  }
+  count[i] = m;
+}
+
+__global__ void kp_fill_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ idx,
+                               const double* __restrict__ val, const int32_t* __restrict__ agg,
+                               const int64_t* __restrict__ kp_ptr, int32_t* __restrict__ kp_idx,
+                               double* __restrict__ kp_val) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t k0 = indptr[i], k1 = indptr[i + 1];
+  int64_t o = kp_ptr[i];
+  int cur = -1;
+  for (;;) {
+    int nxt = 0x7fffffff;
+    for (int64_t k = k0; k < k1; ++k) {
+      const int a = agg[idx[k]];
+      if (a > cur && a < nxt) nxt = a;
+    }
+    if (nxt == 0x7fffffff) break;
+    double s = 0.0;
+    for (int64_t k = k0; k < k1; ++k)
+      if (agg[idx[k]] == nxt) s += val[k];
+    kp_idx[o] = nxt;
+    kp_val[o] = s;
+    ++o;
+    cur = nxt;
+  }
+}
+
 }  // namespace tl
 }  // namespace tmg
 
-extern "C" int tm_twolevel_apply(const tm_twolevel* t, const double* r, double* z, void* stream) {
-  if (!t || !r || !z) return TM_ERR_INVALID;
-  if (t->n < 0 || t->nc < 1 || t->k_nnz < 0) return TM_ERR_INVALID;
-  if (t->n == 0) return TM_OK;
-  if (!t->agg || !t->agg_ptr || !t->agg_perm || !t->kc_inv || !t->kp_indptr || !t->kp_indices || !t->kp_values ||
-      !t->k_indptr || !t->k_indices || !t->k_values || !t->sw || !t->work)
-    return TM_ERR_INVALID;
-  using namespace tmg::tl;
+// count[i] = aggregates among the columns of row i (fill kp_indptr = exclusive
+// scan of it, then call tm_kp_fill)
+extern "C" int tm_kp_count(int64_t n, const int64_t* indptr, const int32_t* indices, const int32_t* agg,
+                           int64_t* count, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
+  if (n == 0) return TM_OK;
+  if (!indptr || !indices || !agg || !count) return TM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  tmg::tl::kp_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, indptr, indices, agg, count);
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+extern "C" int tm_kp_fill(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values,
+                          const int32_t* agg, const int64_t* kp_indptr, int32_t* kp_indices, double* kp_values,
+                          void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
+  if (n == 0) return TM_OK;
+  if (!indptr || !indices || !values || !agg || !kp_indptr || !kp_indices || !kp_values) return TM_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  tmg::tl::kp_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, indptr, indices, values, agg, kp_indptr,
+                                                                      kp_indices, kp_values);
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z, cudaStream_t s) {
+  using namespace tmg::tl;
   const int64_t n = t->n;
   const int32_t nc = t->nc;
   float* s1 = t->work;
@@ -89,4 +261,44 @@ extern "C" int tm_twolevel_apply(const tm_twolevel* t, const double* r, double* 
   gemv_kernel<<<gc, kThreads, 0, s>>>(nc, t->kc_inv, rc2, yc2);
   finish_kernel<<<gn, kThreads, 0, s>>>(n, t->agg, yc, yc2, s1, z);
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+static bool twolevel_ok(const tm_twolevel* t) {
+  return t->n >= 0 && t->nc >= 1 && t->k_nnz >= 0 && t->agg && t->agg_ptr && t->agg_perm && t->kc_inv &&
+         t->kp_indptr && t->kp_indices && t->kp_values && t->k_indptr && t->k_indices && t->k_values && t->sw &&
+         t->work;
+}
+
+extern "C" int64_t tm_fcg_workspace_doubles(void) { return 2 * (int64_t)tmg::tl::kFcgBlocks + 8; }
+
+extern "C" int tm_fcg_twolevel_iterations(const tm_twolevel* t, int64_t a_nnz, const int64_t* a_indptr,
+                                          const int32_t* a_indices, const double* a_values, double* x, double* r,
+                                          double* p, double* q, double* z, double* sc, double* part, int32_t iters,
+                                          void* stream) {
+  if (!t || !twolevel_ok(t) || iters < 0 || a_nnz < 0) return TM_ERR_INVALID;
+  if (!a_indptr || !a_indices || !a_values || !x || !r || !p || !q || !z || !sc || !part) return TM_ERR_INVALID;
+  using namespace tmg::tl;
+  const int64_t n = t->n;
+  if (n == 0 || iters == 0) return TM_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  for (int it = 0; it < iters; ++it) {
+    tmg::launch_spmv<double>(n, a_nnz, a_indptr, a_indices, a_values, p, q, s);
+    fcg_dot_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, p, q, part);
+    fcg_alpha_kernel<<<1, 32, 0, s>>>(part, kFcgBlocks, sc);
+    fcg_xr_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, x, r, p, q, sc);
+    const int st = twolevel_apply_impl(t, r, z, s);
+    if (st != TM_OK) return st;
+    fcg_dot2_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, r, z, q, part);
+    fcg_beta_kernel<<<1, 32, 0, s>>>(part, kFcgBlocks, sc);
+    fcg_p_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, p, z, sc);
+  }
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+extern "C" int tm_twolevel_apply(const tm_twolevel* t, const double* r, double* z, void* stream) {
+  if (!t || !r || !z) return TM_ERR_INVALID;
+  if (t->n < 0 || t->nc < 1 || t->k_nnz < 0) return TM_ERR_INVALID;
+  if (t->n == 0) return TM_OK;
+  if (!twolevel_ok(t)) return TM_ERR_INVALID;
+  return twolevel_apply_impl(t, r, z, static_cast<cudaStream_t>(stream));
 }

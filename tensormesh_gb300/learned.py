@@ -185,19 +185,23 @@ class CoarseSpace:
         self.agg = agg
         nc = int(agg.max()) + 1
         self.nc = nc
-        rows = torch.repeat_interleave(torch.arange(n, device=dev), indptr[1:] - indptr[:-1])
-        # K P: entry (i, c) = sum of K_ij over j in aggregate c
-        key = rows * nc + agg[indices.long()]
-        order = torch.argsort(key, stable=True)
-        uniq, counts = torch.unique_consecutive(key[order], return_counts=True)
-        ptr = torch.zeros(uniq.shape[0] + 1, dtype=torch.int64, device=dev)
-        ptr[1:] = torch.cumsum(counts, 0)
-        kp_vals = segment_sum(ptr, order.contiguous(), values.double().contiguous(), 1)
-        kp_rows = torch.div(uniq, nc, rounding_mode="floor")
-        self.kp_indices = (uniq - kp_rows * nc).to(torch.int32).contiguous()
+        # K P: entry (i, c) = sum of K_ij over j in aggregate c, per row in
+        # ascending aggregate order, each sum in CSR order (tm_kp_count /
+        # tm_kp_fill: one thread per row, no global sort)
+        agg32 = agg.to(torch.int32).contiguous()
+        vals64 = values.double().contiguous()
+        s = _s(dev)
+        cnt = torch.empty(n, dtype=torch.int64, device=dev)
+        _lib.call("tm_kp_count", n, indptr.data_ptr(), indices.data_ptr(), agg32.data_ptr(), cnt.data_ptr(), s)
         self.kp_indptr = torch.zeros(n + 1, dtype=torch.int64, device=dev)
-        self.kp_indptr[1:] = torch.cumsum(torch.bincount(kp_rows, minlength=n), 0)
-        self.kp_values = kp_vals.contiguous()
+        self.kp_indptr[1:] = torch.cumsum(cnt, 0)
+        kp_nnz = int(self.kp_indptr[-1])
+        self.kp_indices = torch.empty(kp_nnz, dtype=torch.int32, device=dev)
+        kp_vals = torch.empty(kp_nnz, dtype=torch.float64, device=dev)
+        _lib.call("tm_kp_fill", n, indptr.data_ptr(), indices.data_ptr(), vals64.data_ptr(), agg32.data_ptr(),
+                  self.kp_indptr.data_ptr(), self.kp_indices.data_ptr(), kp_vals.data_ptr(), s)
+        kp_rows = torch.repeat_interleave(torch.arange(n, device=dev), cnt)
+        self.kp_values = kp_vals
         # K_c = P^T (K P): sum the rows of K P by aggregate
         key2 = agg[kp_rows] * nc + self.kp_indices.long()
         order2 = torch.argsort(key2, stable=True)
@@ -219,7 +223,7 @@ class CoarseSpace:
         self.agg_order = torch.argsort(agg, stable=True)
         self.agg_ptr = torch.zeros(nc + 1, dtype=torch.int64, device=dev)
         self.agg_ptr[1:] = torch.cumsum(torch.bincount(agg, minlength=nc), 0)
-        self.agg32 = agg.to(torch.int32).contiguous()
+        self.agg32 = agg32
         self.agg_order32 = self.agg_order.to(torch.int32).contiguous()
         self.kp_values32 = self.kp_values.float().contiguous()
 
@@ -326,7 +330,28 @@ class LearnedPreconditioner:
 
     def _iterate(self, x, r, p, rz, k: int):
         """k flexible-PCG iterations; x, r, p and rz (0-dim) are updated in
-        place, so the sequence can be captured once and replayed."""
+        place, so the sequence can be captured once and replayed.  FP64
+        systems with the fused operator run them as one C call
+        (tm_fcg_twolevel_iterations: the vector updates and dot products in a
+        few fused kernels, every scalar kept on the device)."""
+        if self._fused is not None and x.dtype == torch.float64:
+            n = x.shape[0]
+            bufs = getattr(self, "_fcg_bufs", None)
+            if bufs is None or bufs[0].shape[0] != n or bufs[0].device != x.device:
+                nd = int(_lib.load().tm_fcg_workspace_doubles())
+                bufs = (torch.empty(n, dtype=torch.float64, device=x.device),
+                        torch.empty(n, dtype=torch.float64, device=x.device),
+                        torch.zeros(8, dtype=torch.float64, device=x.device),
+                        torch.empty(nd, dtype=torch.float64, device=x.device))
+                self._fcg_bufs = bufs
+            q, z, sc, part = bufs
+            A = self.A
+            sc[:1].copy_(rz.reshape(1))
+            _lib.call("tm_fcg_twolevel_iterations", self._fused, A.nnz, A.indptr.data_ptr(), A.indices.data_ptr(),
+                      A.values.data_ptr(), x.data_ptr(), r.data_ptr(), p.data_ptr(), q.data_ptr(), z.data_ptr(),
+                      sc.data_ptr(), part.data_ptr(), int(k), _lib.stream_handle(x.device))
+            rz.copy_(sc[0])
+            return
         rr, pp, rzz = r, p, rz
         for _ in range(k):
             q = self._K(pp)
@@ -334,7 +359,9 @@ class LearnedPreconditioner:
             x.add_(alpha * pp)
             r_new = rr - alpha * q
             z_new = self(r_new)
-            beta = torch.clamp(torch.dot(z_new, r_new - rr) / rzz, min=0.0)
+            # Polak-Ribiere (z, r_new - r_old) with r_new - r_old = -alpha q
+            # (the form without the cancelling subtraction, as the fused path)
+            beta = torch.clamp(-alpha * torch.dot(z_new, q) / rzz, min=0.0)
             rzz = torch.dot(r_new, z_new)
             pp = z_new + beta * pp
             rr = r_new

@@ -4,6 +4,7 @@ network on the CPU (same bf16 rounding points), and what the trained network
 gains inside flexible PCG over the same method without it."""
 import math
 
+import numpy as np
 import pytest
 import torch
 
@@ -157,3 +158,55 @@ def test_solve_hook_and_adjoint_with_two_level_preconditioner():
         out.append((float(J.detach()), kappa.grad.clone()))
     assert abs(out[0][0] - out[1][0]) <= 1e-10 * abs(out[0][0])
     assert float((out[0][1] - out[1][1]).abs().max()) <= 1e-8 * float(out[0][1].abs().max())
+
+
+def test_fused_flexible_cg_matches_the_torch_iteration():
+    """tm_fcg_twolevel_iterations (fused vector updates, device scalars)
+    against a torch restatement of the same iteration: q = K p,
+    alpha = rz / (p, q), x += alpha p, r -= alpha q, z = M r,
+    beta = max(0, -alpha (z, q) / rz), rz = (r, z), p = z + beta p."""
+    K, f, coords = poisson_system(12, 5)
+    pre = LearnedPreconditioner(MPNN(DEV, seed=1), coarse_target=64)
+    pre.setup(K, coords)
+    x = torch.zeros_like(f)
+    r = f.clone()
+    z = pre(r)
+    p = z.clone()
+    rz = torch.dot(r, z)
+    xr, rr, pr, rzr = x.clone(), r.clone(), p.clone(), rz.clone()
+    pre._iterate(x, r, p, rz, 6)
+    for _ in range(6):
+        q = pre._K(pr)
+        alpha = rzr / torch.dot(pr, q)
+        xr += alpha * pr
+        rr -= alpha * q
+        zr = pre(rr)
+        beta = torch.clamp(-alpha * torch.dot(zr, q) / rzr, min=0.0)
+        rzr = torch.dot(rr, zr)
+        pr = zr + beta * pr
+    assert float((x - xr).abs().max() / xr.abs().max()) <= 1e-10
+    assert float((r - rr).abs().max() / rr.abs().max()) <= 1e-8
+    assert abs(float(rz) - float(rzr)) <= 1e-9 * abs(float(rzr))
+
+
+def test_kp_kernels_match_a_sorted_torch_construction():
+    """tm_kp_count / tm_kp_fill give K P exactly as the sort-based
+    construction: per row, aggregates ascending, each sum in CSR order."""
+    from tensormesh_gb300.learned import CoarseSpace
+    K, f, coords = poisson_system(12, 2)
+    C = CoarseSpace(K.indptr, K.indices, K.values, coords, target=32)
+    n = K.shape[0]
+    rows = torch.repeat_interleave(torch.arange(n, device=DEV), K.indptr[1:] - K.indptr[:-1])
+    key = rows * C.nc + C.agg[K.indices.long()]
+    order = torch.argsort(key, stable=True)
+    uniq, counts = torch.unique_consecutive(key[order], return_counts=True)
+    vals = K.values.double()[order].cpu().numpy()
+    ends = np.cumsum(counts.cpu().numpy())
+    starts = ends - counts.cpu().numpy()
+    ref = np.array([np.sum(vals[a:b]) if b - a == 1 else float(np.add.reduce(vals[a:b])) for a, b in zip(starts, ends)])
+    kp_rows = torch.div(uniq, C.nc, rounding_mode="floor")
+    np.testing.assert_array_equal(C.kp_indices.cpu().numpy(), (uniq - kp_rows * C.nc).cpu().numpy())
+    ip = torch.zeros(n + 1, dtype=torch.int64, device=DEV)
+    ip[1:] = torch.cumsum(torch.bincount(kp_rows, minlength=n), 0)
+    assert torch.equal(C.kp_indptr, ip)
+    assert np.max(np.abs(C.kp_values.cpu().numpy() - ref)) <= 1e-14 * np.max(np.abs(ref))
