@@ -369,8 +369,9 @@ int tm_pcg_result(const void* work, int32_t* iters, double* res, double* bnorm, 
  * tm_pcg_jacobi_sell: work is caller-owned device scratch of at least
  * tm_pcg_sell_workspace_bytes(dtype, n, n_pad) bytes (the SELL copy of the
  * values, the preconditioned vectors, per-CTA partial sums).  A slice_ptr
- * that does not cover every row returns TM_ERR_INDEX through tm_pcg_result
- * (nothing is iterated).  Asynchronous on `stream`.
+ * that does not cover every row, or a column index outside [0, n), returns
+ * TM_ERR_INDEX through tm_pcg_result (nothing is iterated).  Asynchronous
+ * on `stream`.
  */
 int64_t tm_sell_plan(int64_t n, const int64_t* indptr, const int32_t* indices, int64_t* slice_ptr,
                      int32_t* out_narrow, void* stream);

@@ -187,14 +187,19 @@ __global__ void sell_fill_kernel(int64_t n, const int64_t* __restrict__ indptr, 
   // pad entries gather a valid column: the row itself, or the last row for
   // the lanes past n of the last slice
   const int32_t pad_col = row < n ? (int32_t)row : (int32_t)(n - 1);
-  bool wide = false;
+  bool wide = false;  // a column outside [0, n), or an offset that does not fit 16 bits
   for (int j = 0; j < L; ++j) {
     const int64_t k = s0 + (int64_t)j * 32 + lane;
     int32_t c = pad_col;
     A v = Tr::zero();
     if (j < len) {
-      c = idx[base + j];
-      v = Tr::in(val[base + j]) * Tr::ld(dinv, c);
+      const int32_t cj = idx[base + j];
+      if (cj < 0 || cj >= n) {
+        wide = true;  // stored as the pad entry; the solve stops with TM_ERR_INDEX
+      } else {
+        c = cj;
+        v = Tr::in(val[base + j]) * Tr::ld(dinv, c);
+      }
     }
     if constexpr (kRel) {
       const long long d = (long long)c - row;
@@ -205,7 +210,7 @@ __global__ void sell_fill_kernel(int64_t n, const int64_t* __restrict__ indptr, 
     }
     sval[k] = Tr::pack(v);
   }
-  if (kRel && __any_sync(0xffffffffu, wide) && lane == 0) atomicExch(&st->status, TM_ERR_INDEX);
+  if (__any_sync(0xffffffffu, wide) && lane == 0) atomicExch(&st->status, TM_ERR_INDEX);
   if (row < n) Tr::st(y, row, Tr::in(x0[row]) / Tr::ld(dinv, row));
 }
 

@@ -139,6 +139,14 @@ def test_sell_plan_of_another_pattern_is_rejected():
     status = lib.tm_pcg_result(ws.buf.data_ptr(), None, None, None, s)
     assert status == _lib.TM_ERR_INDEX
     assert int(torch.count_nonzero(x)) == 0
+    # a column index outside [0, n): rejected the same way, without a gather
+    bad_idx = K_ii.indices.clone()
+    bad_idx[5] = n + 7
+    assert lib.tm_pcg_jacobi_sell(_lib.TM_F64, n, K_ii.indptr.data_ptr(), bad_idx.data_ptr(),
+                                  K_ii.values.data_ptr(), sp.data_ptr(), n_pad, f_i.data_ptr(), x.data_ptr(),
+                                  1e-8, 0.0, 100, 0, ws.buf.data_ptr(), ws.nbytes, s) == 0
+    assert lib.tm_pcg_result(ws.buf.data_ptr(), None, None, None, s) == _lib.TM_ERR_INDEX
+    assert int(torch.count_nonzero(x)) == 0
     # argument checks on the host
     assert lib.tm_pcg_jacobi_sell(_lib.TM_F64, n, K_ii.indptr.data_ptr(), K_ii.indices.data_ptr(),
                                   K_ii.values.data_ptr(), sp.data_ptr(), n_pad, f_i.data_ptr(), x.data_ptr(),
