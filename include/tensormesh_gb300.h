@@ -267,7 +267,9 @@ int tm_twolevel_apply(const tm_twolevel* t, const double* r, double* z, void* st
  * device (graph-capturable, no host synchronisation):
  *   q = A p; alpha = rz / (p, q); x += alpha p; r -= alpha q; z = M r;
  *   beta = max(0, -alpha (z, q) / rz); rz = (r, z); p = z + beta p.
- * A is the FP64 CSR matrix (a_*), M the two-level operator t.  x, r, p are
+ * A is the FP64 CSR matrix (a_indptr, a_indices, a_values), or, when
+ * a_slice_ptr is non-NULL, its tm_sell_fill copy (a_slice_ptr, a_narrow,
+ * a_scol, a_sval), M the two-level operator t.  x, r, p are
  * updated in place; q and z are scratch of n doubles; sc[0] holds rz on
  * entry and on exit (sc: 8 doubles: rz, alpha, beta, (p, q)); part is
  * scratch of tm_fcg_workspace_doubles() doubles.  Dot products reduce in a
@@ -284,8 +286,9 @@ int tm_kp_count(int64_t n, const int64_t* indptr, const int32_t* indices, const 
 int tm_kp_fill(int64_t n, const int64_t* indptr, const int32_t* indices, const double* values, const int32_t* agg,
                const int64_t* kp_indptr, int32_t* kp_indices, double* kp_values, void* stream);
 int tm_fcg_twolevel_iterations(const tm_twolevel* t, int64_t a_nnz, const int64_t* a_indptr, const int32_t* a_indices,
-                               const double* a_values, double* x, double* r, double* p, double* q, double* z,
-                               double* sc, double* part, int32_t iters, void* stream);
+                               const double* a_values, const int64_t* a_slice_ptr, int32_t a_narrow,
+                               const void* a_scol, const double* a_sval, double* x, double* r, double* p, double* q,
+                               double* z, double* sc, double* part, int32_t iters, void* stream);
 
 /*
  * Neo-Hookean energy per element and its displacement gradient per (element,
@@ -380,6 +383,16 @@ int64_t tm_pcg_sell_workspace_bytes(int32_t dtype, int64_t n, int64_t n_pad);
 #define TM_PCG_PIPELINED 1  /* Ghysels-Vanroose pipelined PCG, one barrier; less stable */
 #define TM_PCG_NARROW 2     /* or-ed in: 16-bit column offsets (the plan's out_narrow must be 1;
                                an offset that does not fit returns TM_ERR_INDEX) */
+/* A plain SELL-32 copy of a CSR matrix on a tm_sell_plan slice plan (values
+ * as given: FP64 in double, FP32 in float; scol int16 offsets from the row
+ * when narrow, else int32 columns), and y = A x on it.  *bad_flag (device
+ * int32) is set to 1 when the plan does not cover a row, a column lies
+ * outside [0, n) or an offset does not fit 16 bits. */
+int tm_sell_fill(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices, const void* values,
+                 const int64_t* slice_ptr, int64_t n_pad, int32_t narrow, void* scol, void* sval, int32_t* bad_flag,
+                 void* stream);
+int tm_spmv_sell(int32_t dtype, int64_t n, const int64_t* slice_ptr, int32_t narrow, const void* scol,
+                 const void* sval, const void* x, void* y, void* stream);
 int tm_pcg_jacobi_sell(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices, const void* values,
                        const int64_t* slice_ptr, int64_t n_pad, const void* b, void* x, double rtol, double atol,
                        int32_t maxiter, int32_t method, void* work, int64_t work_bytes, void* stream);

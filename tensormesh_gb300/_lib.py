@@ -41,6 +41,7 @@ EXPORTS = [
     "tm_selftest_barrier_timeout", "tm_pattern_workspace_bytes", "tm_pattern_count", "tm_pattern_fill",
     "tm_sell_plan", "tm_pcg_sell_workspace_bytes", "tm_pcg_jacobi_sell",
     "tm_fcg_workspace_doubles", "tm_fcg_twolevel_iterations", "tm_kp_count", "tm_kp_fill",
+    "tm_sell_fill", "tm_spmv_sell",
 ]
 
 P = ctypes.c_void_p
@@ -137,7 +138,10 @@ def _declare(lib):
         "tm_pcg_jacobi_noalloc": [i64, P, P, P, P, P, ctypes.c_double, ctypes.c_double, i32,
                                   ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_double), P],
         "tm_twolevel_apply": [ctypes.POINTER(TwoLevel), P, P, P],
-        "tm_fcg_twolevel_iterations": [ctypes.POINTER(TwoLevel), i64, P, P, P, P, P, P, P, P, P, P, i32, P],
+        "tm_fcg_twolevel_iterations": [ctypes.POINTER(TwoLevel), i64, P, P, P, P, i32, P, P, P, P, P, P, P, P, P, i32,
+                                       P],
+        "tm_sell_fill": [i32, i64, P, P, P, P, i64, i32, P, P, P, P],
+        "tm_spmv_sell": [i32, i64, P, i32, P, P, P, P, P],
         "tm_kp_count": [i64, P, P, P, P, P],
         "tm_kp_fill": [i64, P, P, P, P, P, P, P, P],
         "tm_neohookean": [i32, i32, i32, P, P, P, i64, P, ctypes.c_double, ctypes.c_double, P, P, P],

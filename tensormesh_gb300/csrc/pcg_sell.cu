@@ -62,6 +62,19 @@ template <> struct SellT<float> {
   static TM_D double to_double(A v) { return (double)v; }
   static TM_D A zero() { return 0.f; }
 };
+template <> struct SellT<double> {  // native FP64 (plain products, no iteration)
+  using A = double;
+  using V = double;
+  static TM_D A ld(const double* p, int64_t i) { return p[i]; }
+  static TM_D void st(double* p, int64_t i, A v) { p[i] = v; }
+  static TM_D A mk(double v) { return v; }
+  static TM_D double pack(A v) { return v; }
+  static TM_D A in(V v) { return v; }
+  static TM_D V out(A v) { return v; }
+  static TM_D A from_double(double d) { return d; }
+  static TM_D double to_double(A v) { return v; }
+  static TM_D A zero() { return 0.0; }
+};
 template <> struct SellT<F2> {
   using A = df64;
   using V = double;
@@ -543,6 +556,70 @@ pcg_sell_kernel(int64_t n, const int64_t* __restrict__ sptr, const CT* __restric
   }
 }
 
+// ---- plain SELL-32 copies and products (y = A x), for solvers that apply A
+// many times outside the PCG kernels (the two-level flexible CG)
+template <class S, class CT>
+__global__ void sell_copy_kernel(int64_t n, const int64_t* __restrict__ indptr, const int32_t* __restrict__ idx,
+                                 const typename SellT<S>::V* __restrict__ val, const int64_t* __restrict__ sptr,
+                                 int64_t n_pad, CT* __restrict__ scol, S* __restrict__ sval, int* bad) {
+  constexpr bool kRel = sizeof(CT) == 2;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t n_slices = (n + 31) >> 5;
+  if (gw >= n_slices) return;
+  const int64_t row = gw * 32 + lane;
+  const int64_t s0 = sptr[gw], s1 = sptr[gw + 1];
+  const int64_t width = s1 - s0;
+  const int64_t len = row < n ? indptr[row + 1] - indptr[row] : 0;
+  bool wrong = s0 < 0 || s1 > n_pad || width < 0 || (width & 31) != 0 || len > (width >> 5);
+  if (__any_sync(0xffffffffu, wrong)) {
+    if (lane == 0) atomicExch(bad, 1);
+    return;
+  }
+  const int L = (int)(width >> 5);
+  const int64_t base = row < n ? indptr[row] : 0;
+  const int32_t pad_col = row < n ? (int32_t)row : (int32_t)(n - 1);
+  for (int j = 0; j < L; ++j) {
+    const int64_t k = s0 + (int64_t)j * 32 + lane;
+    int32_t c = pad_col;
+    S v = S(0);
+    if (j < len) {
+      const int32_t cj = idx[base + j];
+      if (cj < 0 || cj >= n) {
+        wrong = true;
+      } else {
+        c = cj;
+        v = (S)val[base + j];
+      }
+    }
+    if constexpr (kRel) {
+      const long long d = (long long)c - row;
+      wrong = wrong || d < -32768 || d > 32767;
+      scol[k] = (CT)d;
+    } else {
+      scol[k] = c;
+    }
+    sval[k] = v;
+  }
+  if (__any_sync(0xffffffffu, wrong) && lane == 0) atomicExch(bad, 1);
+}
+
+template <class S, class CT>
+__global__ void __launch_bounds__(256) sell_spmv_kernel(int64_t n, const int64_t* __restrict__ sptr,
+                                                         const CT* __restrict__ scol, const S* __restrict__ sval,
+                                                         const S* __restrict__ x, S* __restrict__ y) {
+  using Tr = SellT<S>;
+  using A = typename Tr::A;
+  const int64_t sl = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_slices = (n + 31) >> 5;
+  if (sl >= n_slices) return;  // whole warps leave together
+  A acc[kSellRows];
+  // sell_rows advances slices sl + u * kSellWarps; with kSellRows = 1 only sl
+  sell_rows<S, CT>(sptr, scol, sval, [&](int c) { return Tr::ld(x, c); }, sl, sl + 1, acc);
+  const int64_t row = sl * 32 + (threadIdx.x & 31);
+  if (row < n) Tr::st(y, row, acc[0]);
+}
+
 inline int64_t align256(int64_t b) { return (b + 255) & ~int64_t(255); }
 
 constexpr int kSellMaxBlocks = 4096;
@@ -671,4 +748,64 @@ extern "C" int tm_pcg_jacobi_sell(int32_t dtype, int64_t n, const int64_t* indpt
                                          (const double*)b, (double*)x, rtol, atol, maxiter, method, w, s);
   return tmg::launch_pcg_sell_any<float>(n, indptr, indices, (const float*)values, slice_ptr, n_pad, (const float*)b,
                                      (float*)x, rtol, atol, maxiter, method, w, s);
+}
+
+// A plain SELL-32 copy of a CSR matrix (values as given) on a tm_sell_plan
+// slice plan; scol holds int16 offsets when narrow, else int32 columns.
+extern "C" int tm_sell_fill(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
+                            const void* values, const int64_t* slice_ptr, int64_t n_pad, int32_t narrow, void* scol,
+                            void* sval, int32_t* bad_flag, void* stream) {
+  if (n < 0 || n_pad < 0) return TM_ERR_INVALID;
+  if (n == 0) return TM_OK;
+  if (!indptr || !indices || !values || !slice_ptr || !scol || !sval || !bad_flag) return TM_ERR_INVALID;
+  if (dtype != TM_F32 && dtype != TM_F64) return TM_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int64_t n_slices = (n + 31) >> 5;
+  const unsigned grid = (unsigned)((n_slices * 32 + 255) / 256);
+  if (cudaMemsetAsync(bad_flag, 0, sizeof(int32_t), s) != cudaSuccess) return TM_ERR_CUDA;
+  if (dtype == TM_F64) {
+    if (narrow)
+      tmg::sell_copy_kernel<double, int16_t><<<grid, 256, 0, s>>>(n, indptr, indices, (const double*)values, slice_ptr,
+                                                                   n_pad, (int16_t*)scol, (double*)sval, bad_flag);
+    else
+      tmg::sell_copy_kernel<double, int32_t><<<grid, 256, 0, s>>>(n, indptr, indices, (const double*)values, slice_ptr,
+                                                                   n_pad, (int32_t*)scol, (double*)sval, bad_flag);
+  } else {
+    if (narrow)
+      tmg::sell_copy_kernel<float, int16_t><<<grid, 256, 0, s>>>(n, indptr, indices, (const float*)values, slice_ptr,
+                                                                  n_pad, (int16_t*)scol, (float*)sval, bad_flag);
+    else
+      tmg::sell_copy_kernel<float, int32_t><<<grid, 256, 0, s>>>(n, indptr, indices, (const float*)values, slice_ptr,
+                                                                  n_pad, (int32_t*)scol, (float*)sval, bad_flag);
+  }
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}
+
+// y = A x on a tm_sell_fill copy (dtype of values, x and y; FP64 in native
+// double): one warp per slice, eight entries of each row in flight.
+extern "C" int tm_spmv_sell(int32_t dtype, int64_t n, const int64_t* slice_ptr, int32_t narrow, const void* scol,
+                            const void* sval, const void* x, void* y, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
+  if (n == 0) return TM_OK;
+  if (!slice_ptr || !scol || !sval || !x || !y) return TM_ERR_INVALID;
+  if (dtype != TM_F32 && dtype != TM_F64) return TM_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int64_t n_slices = (n + 31) >> 5;
+  const unsigned grid = (unsigned)((n_slices * 32 + 255) / 256);
+  if (dtype == TM_F64) {
+    if (narrow)
+      tmg::sell_spmv_kernel<double, int16_t><<<grid, 256, 0, s>>>(n, slice_ptr, (const int16_t*)scol,
+                                                                   (const double*)sval, (const double*)x, (double*)y);
+    else
+      tmg::sell_spmv_kernel<double, int32_t><<<grid, 256, 0, s>>>(n, slice_ptr, (const int32_t*)scol,
+                                                                   (const double*)sval, (const double*)x, (double*)y);
+  } else {
+    if (narrow)
+      tmg::sell_spmv_kernel<float, int16_t><<<grid, 256, 0, s>>>(n, slice_ptr, (const int16_t*)scol,
+                                                                  (const float*)sval, (const float*)x, (float*)y);
+    else
+      tmg::sell_spmv_kernel<float, int32_t><<<grid, 256, 0, s>>>(n, slice_ptr, (const int32_t*)scol,
+                                                                  (const float*)sval, (const float*)x, (float*)y);
+  }
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }

@@ -272,17 +272,25 @@ static bool twolevel_ok(const tm_twolevel* t) {
 extern "C" int64_t tm_fcg_workspace_doubles(void) { return 2 * (int64_t)tmg::tl::kFcgBlocks + 8; }
 
 extern "C" int tm_fcg_twolevel_iterations(const tm_twolevel* t, int64_t a_nnz, const int64_t* a_indptr,
-                                          const int32_t* a_indices, const double* a_values, double* x, double* r,
-                                          double* p, double* q, double* z, double* sc, double* part, int32_t iters,
-                                          void* stream) {
+                                          const int32_t* a_indices, const double* a_values,
+                                          const int64_t* a_slice_ptr, int32_t a_narrow, const void* a_scol,
+                                          const double* a_sval, double* x, double* r, double* p, double* q, double* z,
+                                          double* sc, double* part, int32_t iters, void* stream) {
   if (!t || !twolevel_ok(t) || iters < 0 || a_nnz < 0) return TM_ERR_INVALID;
   if (!a_indptr || !a_indices || !a_values || !x || !r || !p || !q || !z || !sc || !part) return TM_ERR_INVALID;
+  const bool sell = a_slice_ptr != nullptr;
+  if (sell && (!a_scol || !a_sval)) return TM_ERR_INVALID;
   using namespace tmg::tl;
   const int64_t n = t->n;
   if (n == 0 || iters == 0) return TM_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   for (int it = 0; it < iters; ++it) {
-    tmg::launch_spmv<double>(n, a_nnz, a_indptr, a_indices, a_values, p, q, s);
+    if (sell) {
+      const int st = tm_spmv_sell(TM_F64, n, a_slice_ptr, a_narrow, a_scol, a_sval, p, q, stream);
+      if (st != TM_OK) return st;
+    } else {
+      tmg::launch_spmv<double>(n, a_nnz, a_indptr, a_indices, a_values, p, q, s);
+    }
     fcg_dot_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, p, q, part);
     fcg_alpha_kernel<<<1, 32, 0, s>>>(part, kFcgBlocks, sc);
     fcg_xr_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, x, r, p, q, sc);

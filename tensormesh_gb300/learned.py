@@ -280,7 +280,25 @@ class LearnedPreconditioner:
         self.w = self.weights()
         self.sw = (self.w.double() * self.G.dinv).to(A.dtype).contiguous()
         self._fused = self._fused_struct() if A.dtype == torch.float64 else None
+        self._sell = self._sell_copy() if A.dtype == torch.float64 else None
         self._setup_key = key
+
+    def _sell_copy(self):
+        """SELL-32 copy of K (FP64 values, 16-bit column offsets where they
+        fit) for the flexible CG's products (tm_sell_fill / tm_spmv_sell)."""
+        from .solve import sell_plan
+        A = self.A
+        sp, n_pad, narrow = sell_plan(A.indptr, A.indices)
+        dev = A.values.device
+        scol = torch.empty(n_pad, dtype=torch.int16 if narrow else torch.int32, device=dev)
+        sval = torch.empty(n_pad, dtype=torch.float64, device=dev)
+        bad = torch.zeros(1, dtype=torch.int32, device=dev)
+        _lib.call("tm_sell_fill", _lib.TM_F64, A.shape[0], A.indptr.data_ptr(), A.indices.data_ptr(),
+                  A.values.detach().contiguous().data_ptr(), sp.data_ptr(), n_pad, int(narrow), scol.data_ptr(),
+                  sval.data_ptr(), bad.data_ptr(), _s(dev))
+        if int(bad.item()) != 0:
+            return None    # a pattern the copy cannot hold: the products stay on the CSR arrays
+        return sp, int(narrow), scol, sval
 
     def _fused_struct(self):
         """ctypes view of the operator for tm_twolevel_apply (the tensors it
@@ -347,9 +365,12 @@ class LearnedPreconditioner:
             q, z, sc, part = bufs
             A = self.A
             sc[:1].copy_(rz.reshape(1))
+            sell = getattr(self, "_sell", None)
+            sp, narrow, scol, sval = sell if sell is not None else (None, 0, None, None)
             _lib.call("tm_fcg_twolevel_iterations", self._fused, A.nnz, A.indptr.data_ptr(), A.indices.data_ptr(),
-                      A.values.data_ptr(), x.data_ptr(), r.data_ptr(), p.data_ptr(), q.data_ptr(), z.data_ptr(),
-                      sc.data_ptr(), part.data_ptr(), int(k), _lib.stream_handle(x.device))
+                      A.values.data_ptr(), _lib.ptr(sp), narrow, _lib.ptr(scol), _lib.ptr(sval), x.data_ptr(),
+                      r.data_ptr(), p.data_ptr(), q.data_ptr(), z.data_ptr(), sc.data_ptr(), part.data_ptr(), int(k),
+                      _lib.stream_handle(x.device))
             rz.copy_(sc[0])
             return
         rr, pp, rzz = r, p, rz

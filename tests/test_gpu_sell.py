@@ -218,3 +218,38 @@ def test_wide_couplings_keep_32_bit_columns(monkeypatch):
                                   _lib.TM_PCG_NARROW, ws.buf.data_ptr(), ws.nbytes, s) == 0
     assert lib.tm_pcg_result(ws.buf.data_ptr(), None, None, None, s) == _lib.TM_ERR_INDEX
     assert int(torch.count_nonzero(x)) == 0
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_plain_sell_copy_and_product(dtype):
+    """tm_sell_fill / tm_spmv_sell: y = A x on the plain SELL-32 copy equals
+    the CSR product, with 16-bit offsets and with 32-bit columns."""
+    K_ii, f_i = poisson(14)
+    n = f_i.shape[0]
+    sp, n_pad, narrow = S.sell_plan(K_ii.indptr, K_ii.indices)
+    assert narrow
+    vals = K_ii.values.to(dtype).contiguous()
+    x = torch.randn(n, dtype=torch.float64, device=DEV).to(dtype)
+    ref = S.spmv_raw(K_ii.indptr, K_ii.indices, vals, x)
+    lib = _lib.load()
+    s = _lib.stream_handle(f_i.device)
+    code = _lib.TM_F64 if dtype == torch.float64 else _lib.TM_F32
+    for nar in (1, 0):
+        scol = torch.empty(n_pad, dtype=torch.int16 if nar else torch.int32, device=DEV)
+        sval = torch.empty(n_pad, dtype=dtype, device=DEV)
+        bad = torch.zeros(1, dtype=torch.int32, device=DEV)
+        assert lib.tm_sell_fill(code, n, K_ii.indptr.data_ptr(), K_ii.indices.data_ptr(), vals.data_ptr(),
+                                sp.data_ptr(), n_pad, nar, scol.data_ptr(), sval.data_ptr(), bad.data_ptr(), s) == 0
+        assert int(bad.item()) == 0
+        y = torch.empty_like(x)
+        assert lib.tm_spmv_sell(code, n, sp.data_ptr(), nar, scol.data_ptr(), sval.data_ptr(), x.data_ptr(),
+                                y.data_ptr(), s) == 0
+        tol = 1e-14 if dtype == torch.float64 else 1e-6
+        assert float((y - ref).abs().max() / ref.abs().max()) <= tol
+    # a column outside [0, n) raises the flag
+    bad_idx = K_ii.indices.clone()
+    bad_idx[3] = -1
+    bad = torch.zeros(1, dtype=torch.int32, device=DEV)
+    assert lib.tm_sell_fill(code, n, K_ii.indptr.data_ptr(), bad_idx.data_ptr(), vals.data_ptr(), sp.data_ptr(),
+                            n_pad, 1, scol.data_ptr(), sval.data_ptr(), bad.data_ptr(), s) == 0
+    assert int(bad.item()) == 1
