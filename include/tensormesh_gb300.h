@@ -257,6 +257,13 @@ typedef struct tm_twolevel {
   const float* k_values;
   const float* sw;            /* [n] smoother weights w_i / K_ii */
   float* work;
+  /* optional SELL-32 copy of K in float32 (tm_sell_fill); NULL k_slice_ptr
+   * = the products use the CSR arrays above */
+  const int64_t* k_slice_ptr;
+  const void* k_scol;
+  const float* k_sval;
+  int32_t k_narrow;
+  int32_t pad1;
 } tm_twolevel;
 
 int tm_twolevel_apply(const tm_twolevel* t, const double* r, double* z, void* stream);

@@ -256,7 +256,12 @@ static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z,
   restrict_kernel<double><<<gc, kThreads, 0, s>>>(nc, t->agg_ptr, t->agg_perm, r, rc);
   gemv_kernel<<<gc, kThreads, 0, s>>>(nc, t->kc_inv, rc, yc);
   smooth_kernel<<<gn, kThreads, 0, s>>>(n, t->kp_indptr, t->kp_indices, t->kp_values, yc, r, t->sw, s1);
-  tmg::launch_spmv<float>(n, t->k_nnz, t->k_indptr, t->k_indices, t->k_values, s1, r2, s);
+  if (t->k_slice_ptr) {
+    const int st = tm_spmv_sell(TM_F32, n, t->k_slice_ptr, t->k_narrow, t->k_scol, t->k_sval, s1, r2, s);
+    if (st != TM_OK) return st;
+  } else {
+    tmg::launch_spmv<float>(n, t->k_nnz, t->k_indptr, t->k_indices, t->k_values, s1, r2, s);
+  }
   restrict_kernel<float><<<gc, kThreads, 0, s>>>(nc, t->agg_ptr, t->agg_perm, r2, rc2);
   gemv_kernel<<<gc, kThreads, 0, s>>>(nc, t->kc_inv, rc2, yc2);
   finish_kernel<<<gn, kThreads, 0, s>>>(n, t->agg, yc, yc2, s1, z);
@@ -266,7 +271,7 @@ static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z,
 static bool twolevel_ok(const tm_twolevel* t) {
   return t->n >= 0 && t->nc >= 1 && t->k_nnz >= 0 && t->agg && t->agg_ptr && t->agg_perm && t->kc_inv &&
          t->kp_indptr && t->kp_indices && t->kp_values && t->k_indptr && t->k_indices && t->k_values && t->sw &&
-         t->work;
+         t->work && (!t->k_slice_ptr || (t->k_scol && t->k_sval));
 }
 
 extern "C" int64_t tm_fcg_workspace_doubles(void) { return 2 * (int64_t)tmg::tl::kFcgBlocks + 8; }

@@ -279,8 +279,8 @@ class LearnedPreconditioner:
         self.coarse = CoarseSpace(A.indptr, A.indices, A.values.detach(), coords, self.coarse_target)
         self.w = self.weights()
         self.sw = (self.w.double() * self.G.dinv).to(A.dtype).contiguous()
-        self._fused = self._fused_struct() if A.dtype == torch.float64 else None
         self._sell = self._sell_copy() if A.dtype == torch.float64 else None
+        self._fused = self._fused_struct() if A.dtype == torch.float64 else None
         self._setup_key = key
 
     def _sell_copy(self):
@@ -298,7 +298,9 @@ class LearnedPreconditioner:
                   sval.data_ptr(), bad.data_ptr(), _s(dev))
         if int(bad.item()) != 0:
             return None    # a pattern the copy cannot hold: the products stay on the CSR arrays
-        return sp, int(narrow), scol, sval
+        # the float32 copy for the smoother's product shares the column array
+        sval32 = sval.float()
+        return sp, int(narrow), scol, sval, sval32
 
     def _fused_struct(self):
         """ctypes view of the operator for tm_twolevel_apply (the tensors it
@@ -316,6 +318,10 @@ class LearnedPreconditioner:
         t.k_nnz = int(G.values32.shape[0])
         t.k_indptr, t.k_indices, t.k_values = A.indptr.data_ptr(), A.indices.data_ptr(), G.values32.data_ptr()
         t.sw, t.work = self._sw32.data_ptr(), self._work.data_ptr()
+        sell = getattr(self, "_sell", None)
+        if sell is not None:
+            t.k_slice_ptr, t.k_scol, t.k_sval, t.k_narrow = (sell[0].data_ptr(), sell[2].data_ptr(),
+                                                             sell[4].data_ptr(), sell[1])
         return t
 
     def weights(self, keep: bool = False):
@@ -366,7 +372,7 @@ class LearnedPreconditioner:
             A = self.A
             sc[:1].copy_(rz.reshape(1))
             sell = getattr(self, "_sell", None)
-            sp, narrow, scol, sval = sell if sell is not None else (None, 0, None, None)
+            sp, narrow, scol, sval = sell[:4] if sell is not None else (None, 0, None, None)
             _lib.call("tm_fcg_twolevel_iterations", self._fused, A.nnz, A.indptr.data_ptr(), A.indices.data_ptr(),
                       A.values.data_ptr(), _lib.ptr(sp), narrow, _lib.ptr(scol), _lib.ptr(sval), x.data_ptr(),
                       r.data_ptr(), p.data_ptr(), q.data_ptr(), z.data_ptr(), sc.data_ptr(), part.data_ptr(), int(k),
