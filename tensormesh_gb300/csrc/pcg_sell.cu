@@ -8,16 +8,19 @@
 // residual on 3D Poisson, and in double-float on ill-conditioned elasticity,
 // so they are opt-in.
 //
-// Same contract as tm_pcg_jacobi (the reference's Jacobi-preconditioned CG,
-// sparse/solve/torch_solve.py:24-59 and 130-248: M = diag(A)^-1 with a
-// missing or zero diagonal taken as 1, stop when ||r|| <= max(rtol ||b||, atol)
-// on the recurrence residual), different data path:
+// Same contract as tm_pcg_jacobi (the reference's Jacobi preconditioner,
+// sparse/solve/torch_solve.py:24-59, M = diag(A)^-1 with a missing or zero
+// diagonal taken as 1, inside its CG loop, torch_solve.py:70-128; stop when
+// ||r|| <= max(rtol ||b||, atol) on the recurrence residual), different data
+// path:
 //
 // * SELL-32 layout: rows are grouped in slices of 32 consecutive rows; a
 //   slice stores its rows' entries column-major, padded to its longest row
 //   (pad entries: column = the row itself, value 0).  Entry j of row
 //   32 s + l sits at slice_ptr[s] + 32 j + l, so the 32 lanes of a warp read
-//   one contiguous 128 B (index) and 256 B (df64 value) run per entry.
+//   one contiguous run of column data (128 B of int32 columns, or 64 B of
+//   int16 offsets from the row where every offset fits) and one of values
+//   (256 B in double-float) per entry.
 // * The preconditioner is folded into the stored values: the copy holds
 //   A M (column j scaled by M_jj), so the product n = A M w that the
 //   pipelined recurrence needs is one gather of w per entry.
