@@ -627,20 +627,31 @@ inline int64_t align256(int64_t b) { return (b + 255) & ~int64_t(255); }
 
 constexpr int kSellMaxBlocks = 4096;
 
+// Cooperative grid: two CTAs per SM when each gets at least kSlicesPerCta
+// slices, else one.  Small systems are bound by the two grid barriers and
+// the partial-sum reads per iteration, which cost more with more CTAs
+// (us per iteration, 304 / 152 CTAs: 2D 65k rows 23.2 / 16.3, 3D 64^3 31.2 /
+// 27.3, 96^3 64.4 / 80.1, 128^3 127 / 172).
+constexpr int kSlicesPerCta = 48;
+
 template <class K>
-int sell_blocks(K kern) {
+int sell_blocks(K kern, int64_t n_slices) {
   int dev = 0, sms = 0, per_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSellThreads, 0);
-  return min(kSellMaxBlocks, sms * min(per_sm, 2));
+  int nb = sms * min(per_sm, 2);
+  if (n_slices < (int64_t)kSlicesPerCta * nb) nb = min(nb, sms);
+  return min(kSellMaxBlocks, nb);
 }
 
 template <class S, class CT>
 int launch_pcg_sell(int64_t n, const int64_t* indptr, const int32_t* indices, const typename SellT<S>::V* values,
                     const int64_t* sptr, int64_t n_pad, const typename SellT<S>::V* b, typename SellT<S>::V* x,
                     double rtol, double atol, int maxiter, bool pipe, char* w, cudaStream_t s) {
-  const int nb = pipe ? sell_blocks(pcg_sell_kernel<S, CT>) : sell_blocks(pcg_sell_hs_kernel<S, CT>);
+  const int64_t n_slices_all = (n + 31) >> 5;
+  const int nb = pipe ? sell_blocks(pcg_sell_kernel<S, CT>, n_slices_all)
+                      : sell_blocks(pcg_sell_hs_kernel<S, CT>, n_slices_all);
   if (nb <= 0) return TM_ERR_CUDA;
   PcgState* st = reinterpret_cast<PcgState*>(w);
   char* q = w + 256;
