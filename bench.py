@@ -215,14 +215,24 @@ def run_ours(args):
     t_init = time.perf_counter()
     torch.zeros(1, device=dev).sum().item()          # CUDA context + allocator warm
     init_s = time.perf_counter() - t_init
-    t_setup = time.perf_counter()
-    mesh = tg.Mesh.gen_unit_cube(N_CELLS, device=dev)
-    kappa_h = torch.from_numpy(np.exp(log_kappa_blocks(N_CELLS, BLOCKS, SEED)))
-    kappa = kappa_h.to(dev)
 
     class KappaLaplace(tg.ElementAssembler):
         def forward(self, gradu, gradv, kappa):
             return kappa * (gradu @ gradv)
+
+    # first use of the library kernels the set-up calls (torch's sorts and
+    # scans, the project's own kernels): on a fresh machine their code is
+    # paged in from disk here, which a 4^3 mesh shows apart from the set-up
+    t_first = time.perf_counter()
+    tiny = tg.Mesh.gen_unit_cube(4, device=dev)
+    KappaLaplace.from_mesh(tiny, quadrature_order=1)(tiny.points, element_data={
+        "kappa": torch.ones(tiny.cells["tetra"].shape[0], dtype=torch.float64, device=dev)})
+    torch.cuda.synchronize()
+    first_use_s = time.perf_counter() - t_first
+    t_setup = time.perf_counter()
+    mesh = tg.Mesh.gen_unit_cube(N_CELLS, device=dev)
+    kappa_h = torch.from_numpy(np.exp(log_kappa_blocks(N_CELLS, BLOCKS, SEED)))
+    kappa = kappa_h.to(dev)
 
     asm = KappaLaplace.from_mesh(mesh, quadrature_order=1)
     torch.cuda.synchronize()
@@ -621,6 +631,7 @@ def run_ours(args):
                        "autotune_ms": {str(t["candidate"]): round(t.get("ms", -1), 4) for t in tuned["table"]},
                        "setup_seconds": round(setup_s, 3),
                        "setup_split_seconds": {"cuda_and_torch_init": round(init_s, 3),
+                                               "first_use_of_library_kernels_4cube": round(first_use_s, 3),
                                                **{k: round(v, 3) for k, v in topo.timings.items()}}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
