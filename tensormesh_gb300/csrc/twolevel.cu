@@ -15,19 +15,41 @@ namespace tl {
 
 constexpr int kThreads = 256;
 
+// Loads in flight per lane in the restriction and the coarse matvec: the
+// index loads of a round are all issued before the value loads that depend
+// on them.
+constexpr int kTlIlp = 8;
+
+// rc[c] = sum of r over aggregate c: lane l adds entries l, l + 32, ... of
+// the aggregate in that order, then a shuffle tree (deterministic).
 template <class T>
 __global__ void restrict_kernel(int32_t nc, const int64_t* __restrict__ ptr, const int32_t* __restrict__ perm,
                                 const T* __restrict__ r, float* __restrict__ rc) {
   const int c = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (c >= nc) return;  // the whole warp leaves together
+  const int64_t k1 = ptr[c + 1];
   float s = 0.f;
-  for (int64_t k = ptr[c] + lane; k < ptr[c + 1]; k += 32) s += (float)r[perm[k]];
+  for (int64_t kb = ptr[c] + lane; kb < k1; kb += 32 * kTlIlp) {
+    int id[kTlIlp];
+#pragma unroll
+    for (int u = 0; u < kTlIlp; ++u) id[u] = kb + 32 * u < k1 ? __ldg(perm + kb + 32 * u) : -1;
+    T v[kTlIlp];
+#pragma unroll
+    for (int u = 0; u < kTlIlp; ++u) v[u] = id[u] >= 0 ? r[id[u]] : T(0);
+#pragma unroll
+    for (int u = 0; u < kTlIlp; ++u)
+      if (id[u] >= 0) s += (float)v[u];
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) rc[c] = s;
 }
 
+// y = A x with A dense nc x nc (row-major), one warp per row.  kVec (nc a
+// multiple of 4 and A 16-byte aligned): the row is read as float4, lane l
+// taking quads l, l + 32, ...; kVecX: x is 16-byte aligned too.
+template <bool kVec, bool kVecX>
 __global__ void gemv_kernel(int32_t nc, const float* __restrict__ A, const float* __restrict__ x,
                             float* __restrict__ y) {
   const int row = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
@@ -35,10 +57,45 @@ __global__ void gemv_kernel(int32_t nc, const float* __restrict__ A, const float
   if (row >= nc) return;
   const float* a = A + (int64_t)row * nc;
   float s = 0.f;
-  for (int j = lane; j < nc; j += 32) s += a[j] * x[j];
+  if constexpr (kVec) {
+    const float4* a4 = reinterpret_cast<const float4*>(a);
+    const int n4 = nc >> 2;
+    for (int jb = lane; jb < n4; jb += 32 * kTlIlp) {
+      float4 v[kTlIlp];
+#pragma unroll
+      for (int u = 0; u < kTlIlp; ++u) v[u] = jb + 32 * u < n4 ? __ldg(a4 + jb + 32 * u) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int u = 0; u < kTlIlp; ++u) {
+        const int j = jb + 32 * u;
+        if (j < n4) {
+          float4 xv;
+          if constexpr (kVecX) {
+            xv = __ldg(reinterpret_cast<const float4*>(x) + j);
+          } else {
+            xv = make_float4(__ldg(x + 4 * j), __ldg(x + 4 * j + 1), __ldg(x + 4 * j + 2), __ldg(x + 4 * j + 3));
+          }
+          s = fmaf(v[u].x, xv.x, s);
+          s = fmaf(v[u].y, xv.y, s);
+          s = fmaf(v[u].z, xv.z, s);
+          s = fmaf(v[u].w, xv.w, s);
+        }
+      }
+    }
+  } else {
+    for (int j = lane; j < nc; j += 32) s += a[j] * x[j];
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) y[row] = s;
+}
+
+inline void launch_gemv(int32_t nc, const float* A, const float* x, float* y, cudaStream_t s) {
+  const int grid = (nc + kThreads / 32 - 1) / (kThreads / 32);
+  const bool vec = (nc & 3) == 0 && ((uintptr_t)A & 15u) == 0;
+  const bool vecx = ((uintptr_t)x & 15u) == 0;
+  if (vec && vecx) gemv_kernel<true, true><<<grid, kThreads, 0, s>>>(nc, A, x, y);
+  else if (vec) gemv_kernel<true, false><<<grid, kThreads, 0, s>>>(nc, A, x, y);
+  else gemv_kernel<false, false><<<grid, kThreads, 0, s>>>(nc, A, x, y);
 }
 
 __global__ void smooth_kernel(int64_t n, const int64_t* __restrict__ kp_ptr, const int32_t* __restrict__ kp_idx,
@@ -123,25 +180,6 @@ __global__ void __launch_bounds__(kFcgThreads) fcg_xr_kernel(int64_t n, double* 
   }
 }
 
-// part[b] = share of (r, z), part[nb + b] = share of (z, q)
-__global__ void __launch_bounds__(kFcgThreads) fcg_dot2_kernel(int64_t n, const double* __restrict__ r,
-                                                                const double* __restrict__ z,
-                                                                const double* __restrict__ q, double* part) {
-  __shared__ double red[32];
-  double a = 0.0, c = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double zi = z[i];
-    a = fma(r[i], zi, a);
-    c = fma(zi, q[i], c);
-  }
-  a = fcg_block_sum(a, red);
-  c = fcg_block_sum(c, red);
-  if (threadIdx.x == 0) {
-    part[blockIdx.x] = a;
-    part[gridDim.x + blockIdx.x] = c;
-  }
-}
-
 // Polak-Ribiere: beta = max(0, (z, r_new - r_old) / rz_old) with
 // r_new - r_old = -alpha q; then rz = (r_new, z)
 __global__ void fcg_beta_kernel(const double* part, int nb, double* sc) {
@@ -152,6 +190,33 @@ __global__ void fcg_beta_kernel(const double* part, int nb, double* sc) {
     const double b = rz != 0.0 ? -sc[1] * zq / rz : 0.0;
     sc[2] = b > 0.0 ? b : 0.0;
     sc[0] = rzn;
+  }
+}
+
+// The application's last step fused with the dot products that follow it:
+// z = P (y_c - y_c2) + s, and the CTA's shares of (r, z) into part[b] and of
+// (z, q) into part[nb + b] (grid-stride rows, the CTA's fixed tree).
+__global__ void __launch_bounds__(kFcgThreads) finish_dot2_kernel(int64_t n, const int32_t* __restrict__ agg,
+                                                                   const float* __restrict__ yc,
+                                                                   const float* __restrict__ yc2,
+                                                                   const float* __restrict__ s1,
+                                                                   const double* __restrict__ r,
+                                                                   const double* __restrict__ q,
+                                                                   double* __restrict__ z, double* part) {
+  __shared__ double red[32];
+  double a = 0.0, c = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int g = agg[i];
+    const double zi = (double)((yc[g] - yc2[g]) + s1[i]);
+    z[i] = zi;
+    a = fma(r[i], zi, a);
+    c = fma(zi, q[i], c);
+  }
+  a = fcg_block_sum(a, red);
+  c = fcg_block_sum(c, red);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = a;
+    part[gridDim.x + blockIdx.x] = c;
   }
 }
 
@@ -215,6 +280,7 @@ __global__ void kp_fill_kernel(int64_t n, const int64_t* __restrict__ indptr, co
 }
 
 }  // namespace tl
+
 }  // namespace tmg
 
 // count[i] = aggregates among the columns of row i (fill kp_indptr = exclusive
@@ -241,7 +307,10 @@ extern "C" int tm_kp_fill(int64_t n, const int64_t* indptr, const int32_t* indic
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
 
-static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z, cudaStream_t s) {
+// z = M r.  With q_dot and part (the flexible CG), the last step also forms
+// the partial sums of (r, z) and (z, q_dot) for fcg_beta_kernel.
+static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z, cudaStream_t s,
+                               const double* q_dot = nullptr, double* part = nullptr) {
   using namespace tmg::tl;
   const int64_t n = t->n;
   const int32_t nc = t->nc;
@@ -254,7 +323,7 @@ static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z,
   const int gc = (nc + kThreads / 32 - 1) / (kThreads / 32);
   const int gn = (int)((n + kThreads - 1) / kThreads);
   restrict_kernel<double><<<gc, kThreads, 0, s>>>(nc, t->agg_ptr, t->agg_perm, r, rc);
-  gemv_kernel<<<gc, kThreads, 0, s>>>(nc, t->kc_inv, rc, yc);
+  launch_gemv(nc, t->kc_inv, rc, yc, s);
   smooth_kernel<<<gn, kThreads, 0, s>>>(n, t->kp_indptr, t->kp_indices, t->kp_values, yc, r, t->sw, s1);
   if (t->k_slice_ptr) {
     const int st = tm_spmv_sell(TM_F32, n, t->k_slice_ptr, t->k_narrow, t->k_scol, t->k_sval, s1, r2, s);
@@ -263,8 +332,11 @@ static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z,
     tmg::launch_spmv<float>(n, t->k_nnz, t->k_indptr, t->k_indices, t->k_values, s1, r2, s);
   }
   restrict_kernel<float><<<gc, kThreads, 0, s>>>(nc, t->agg_ptr, t->agg_perm, r2, rc2);
-  gemv_kernel<<<gc, kThreads, 0, s>>>(nc, t->kc_inv, rc2, yc2);
-  finish_kernel<<<gn, kThreads, 0, s>>>(n, t->agg, yc, yc2, s1, z);
+  launch_gemv(nc, t->kc_inv, rc2, yc2, s);
+  if (q_dot)
+    finish_dot2_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, t->agg, yc, yc2, s1, r, q_dot, z, part);
+  else
+    finish_kernel<<<gn, kThreads, 0, s>>>(n, t->agg, yc, yc2, s1, z);
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
 
@@ -299,9 +371,8 @@ extern "C" int tm_fcg_twolevel_iterations(const tm_twolevel* t, int64_t a_nnz, c
     fcg_dot_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, p, q, part);
     fcg_alpha_kernel<<<1, 32, 0, s>>>(part, kFcgBlocks, sc);
     fcg_xr_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, x, r, p, q, sc);
-    const int st = twolevel_apply_impl(t, r, z, s);
+    const int st = twolevel_apply_impl(t, r, z, s, q, part);
     if (st != TM_OK) return st;
-    fcg_dot2_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, r, z, q, part);
     fcg_beta_kernel<<<1, 32, 0, s>>>(part, kFcgBlocks, sc);
     fcg_p_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, p, z, sc);
   }
