@@ -446,6 +446,17 @@ int tm_pattern_fill(const int32_t* elements, int64_t n_elements, int32_t n_basis
                     const int64_t* indptr, int32_t* out_indices, int64_t* out_slots, void* stream);
 
 /*
+ * Morton (Z-order) keys of n points in dim <= 3 dimensions (coords [n][dim]
+ * float64, lo / hi [dim] the bounding box, on the device): coordinate d is
+ * quantised to q = rint((x - lo_d) / max(hi_d - lo_d, 1e-300) * (2^bits - 1))
+ * and bit b of q is bit b * dim + d of keys[i] (bits * dim <= 63).  Used by
+ * the octree partition of the two-level coarse space (no counterpart in the
+ * reference).
+ */
+int tm_morton_keys(int64_t n, int32_t dim, const double* coords, const double* lo, const double* hi, int32_t bits,
+                   int64_t* keys, void* stream);
+
+/*
  * Self-test of the bounded grid barrier the PCG kernels use (no counterpart
  * in the reference: the reference has no device-side waits).  Launches
  * n_blocks cooperative CTAs of which one never arrives at the barrier; the

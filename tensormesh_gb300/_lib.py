@@ -39,6 +39,7 @@ EXPORTS = [
     "tm_mpnn_layer_bwd", "tm_mpnn_input_bwd", "tm_gather_axpy_f32",
     "tm_pcg_jacobi_noalloc", "tm_twolevel_apply", "tm_neohookean", "tm_facet_load",
     "tm_selftest_barrier_timeout", "tm_pattern_workspace_bytes", "tm_pattern_count", "tm_pattern_fill",
+    "tm_morton_keys",
     "tm_sell_plan", "tm_pcg_sell_workspace_bytes", "tm_pcg_jacobi_sell",
     "tm_fcg_workspace_doubles", "tm_fcg_twolevel_iterations", "tm_kp_count", "tm_kp_fill",
     "tm_sell_fill", "tm_spmv_sell",
@@ -150,6 +151,7 @@ def _declare(lib):
         "tm_selftest_barrier_timeout": [i32, i64, ctypes.POINTER(i32), P, P],
         "tm_pattern_count": [P, i64, i32, i64, P, P, P],
         "tm_pattern_fill": [P, i64, i32, i64, P, P, P, P, P],
+        "tm_morton_keys": [i64, i32, P, P, P, i32, P, P],
         "tm_pcg_jacobi_sell": [i32, i64, P, P, P, P, i64, P, P, ctypes.c_double, ctypes.c_double, i32, i32, P, i64,
                                P],
     }

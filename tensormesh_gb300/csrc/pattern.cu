@@ -266,3 +266,34 @@ extern "C" int tm_pattern_fill(const int32_t* elements, int64_t n_elements, int3
   }
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
+
+// ---- Morton (Z-order) keys of points, for the spatial partitions ---------
+// Point i, coordinate d is quantised to q = rint((x - lo_d) / max(hi_d - lo_d,
+// 1e-300) * (2^bits - 1)) (IEEE double, round half to even) and bit b of q
+// goes to bit b D + d of the key: the same arithmetic as the torch
+// restatement this replaces, so the keys are identical.
+namespace tmg {
+__global__ void morton_keys_kernel(int64_t n, int dim, const double* __restrict__ x, const double* __restrict__ lo,
+                                   const double* __restrict__ hi, int bits, int64_t* __restrict__ keys) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double scale = (double)((1ll << bits) - 1);
+  unsigned long long key = 0ull;
+  for (int d = 0; d < dim; ++d) {
+    const double span = fmax(hi[d] - lo[d], 1e-300);
+    const unsigned long long q = (unsigned long long)(long long)rint((x[i * dim + d] - lo[d]) / span * scale);
+    for (int b = 0; b < bits; ++b) key |= ((q >> b) & 1ull) << (b * dim + d);
+  }
+  keys[i] = (int64_t)key;
+}
+}  // namespace tmg
+
+extern "C" int tm_morton_keys(int64_t n, int32_t dim, const double* coords, const double* lo, const double* hi,
+                              int32_t bits, int64_t* keys, void* stream) {
+  if (n < 0 || dim < 1 || dim > 3 || bits < 1 || bits * dim > 63) return TM_ERR_INVALID;
+  if (n == 0) return TM_OK;
+  if (!coords || !lo || !hi || !keys) return TM_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  tmg::morton_keys_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, dim, coords, lo, hi, bits, keys);
+  return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
+}

@@ -47,23 +47,35 @@ def _s(dev):
 
 
 class Graph:
-    """Normalised operator of one SPD CSR matrix (float32)."""
+    """Normalised operator of one SPD CSR matrix (float32): D^-1 for the
+    smoother and, formed on first use (the network's edge weights only),
+    the off-diagonal part of D^-1/2 A D^-1/2."""
 
     def __init__(self, indptr, indices, values):
         self.indptr, self.indices = indptr, indices
         n = indptr.shape[0] - 1
         self.n = n
+        self.device = values.device
+        self._values = values
         dev = values.device
         rows = torch.repeat_interleave(torch.arange(n, device=dev), indptr[1:] - indptr[:-1])
-        diag = torch.zeros(n, dtype=torch.float64, device=dev).index_put_(
-            (rows[rows == indices.long()],), values.double()[rows == indices.long()])
-        diag = torch.where(diag > 0, diag, torch.ones_like(diag))
-        self.dinv_sqrt = (1.0 / diag.sqrt()).float().contiguous()
-        self.dinv = (1.0 / diag).contiguous()                          # FP64
-        a = values.double() * (1.0 / diag.sqrt())[rows] * (1.0 / diag.sqrt())[indices.long()]
-        a = torch.where(rows == indices.long(), torch.zeros_like(a), a)
-        self.aoff = a.float().contiguous()
+        on_diag = rows == indices.long()
+        diag = torch.zeros(n, dtype=torch.float64, device=dev).index_put_((rows[on_diag],), values.double()[on_diag])
+        self._diag = torch.where(diag > 0, diag, torch.ones_like(diag))
+        self.dinv = (1.0 / self._diag).contiguous()                    # FP64
         self.values32 = values.float().contiguous()
+        self._aoff = None
+
+    @property
+    def aoff(self):
+        if self._aoff is None:
+            n, dev = self.n, self.device
+            rows = torch.repeat_interleave(torch.arange(n, device=dev), self.indptr[1:] - self.indptr[:-1])
+            cols = self.indices.long()
+            ds = 1.0 / self._diag.sqrt()
+            a = self._values.double() * ds[rows] * ds[cols]
+            self._aoff = torch.where(rows == cols, torch.zeros_like(a), a).float().contiguous()
+        return self._aoff
 
 
 class MPNN:
@@ -328,8 +340,8 @@ class LearnedPreconditioner:
         """Smoother weights w (float32 [n]); with keep=True also (y, saved)."""
         G = self.G
         if not self.use_network:
-            return torch.ones(G.n, dtype=torch.float32, device=G.aoff.device)
-        x = torch.ones(G.n, dtype=torch.float32, device=G.aoff.device)
+            return torch.ones(G.n, dtype=torch.float32, device=G.device)
+        x = torch.ones(G.n, dtype=torch.float32, device=G.device)
         if keep:
             y, saved = self.model.forward(G, x, keep=True)
             return 0.5 + torch.sigmoid(y), (y, saved)

@@ -157,6 +157,26 @@ def rcb_partition(coords: torch.Tensor, n_levels: int = None, n_parts: int = Non
     return part
 
 
+def morton_keys(c: torch.Tensor, lo: torch.Tensor, hi: torch.Tensor, bits: int) -> torch.Tensor:
+    """Z-order keys of the float64 points c [N, D]: coordinate d quantised to
+    q = round((x - lo_d) / max(hi_d - lo_d, 1e-300) * (2^bits - 1)) (half to
+    even), bit b of q at key bit b D + d.  One kernel on the device
+    (tm_morton_keys); CPU tensors (host-side planning) take the same
+    arithmetic in torch."""
+    N, D = c.shape
+    if c.is_cuda:
+        key = torch.empty(N, dtype=torch.int64, device=c.device)
+        _lib.call("tm_morton_keys", N, D, c.data_ptr(), lo.data_ptr(), hi.data_ptr(), bits, key.data_ptr(),
+                  _lib.stream_handle(c.device))
+        return key
+    q = ((c - lo) / torch.clamp(hi - lo, min=1e-300) * ((1 << bits) - 1)).round().long()
+    key = torch.zeros(N, dtype=torch.int64, device=c.device)
+    for b in range(bits):
+        for d in range(D):
+            key |= ((q[:, d] >> b) & 1) << (b * D + d)
+    return key
+
+
 def morton_parts(coords: torch.Tensor, target: int) -> torch.Tensor:
     """Spatially compact parts of about ``target`` points: the cells of an
     octree (quadtree in 2D) over the bounding box, refined where a cell holds
@@ -168,14 +188,10 @@ def morton_parts(coords: torch.Tensor, target: int) -> torch.Tensor:
     dev = coords.device
     if N == 0:
         return torch.zeros(0, dtype=torch.int64, device=dev)
-    c = coords.to(torch.float64)
-    lo, hi = c.min(0).values, c.max(0).values
+    c = coords.to(torch.float64).contiguous()
+    lo, hi = c.min(0).values.contiguous(), c.max(0).values.contiguous()
     bits = 63 // D
-    q = ((c - lo) / torch.clamp(hi - lo, min=1e-300) * ((1 << bits) - 1)).round().long()
-    key = torch.zeros(N, dtype=torch.int64, device=dev)
-    for b in range(bits):
-        for d in range(D):
-            key |= ((q[:, d] >> b) & 1) << (b * D + d)
+    key = morton_keys(c, lo, hi, bits)
     order = torch.argsort(key, stable=True)
     k = key[order]
     level0 = max(0, min(bits, int(math.floor(math.log(max(1.0, N / target)) / math.log(2 ** D)))))

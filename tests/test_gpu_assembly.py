@@ -224,3 +224,22 @@ def test_pattern_kernels_match_host_definition(etype):
         assert torch.equal(dev.indptr.cpu(), host.indptr)
         assert torch.equal(dev.indices.cpu(), host.indices)
         assert torch.equal(dev.slots.cpu(), host.slots)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_morton_key_kernel_matches_host_definition(dim):
+    """tm_morton_keys against the torch definition of morton_keys on the
+    host, bit for bit: random points, a regular grid (ties of the
+    quantisation round half to even) and a degenerate axis (zero span)."""
+    from tensormesh_gb300.plan import morton_keys, morton_parts
+    g = torch.Generator().manual_seed(dim)
+    grid = torch.stack(torch.meshgrid(*[torch.arange(9, dtype=torch.float64) / 8] * dim, indexing="ij"), -1)
+    flat = torch.rand(500, dim, generator=g, dtype=torch.float64)
+    flat[:, 0] = 0.25
+    for c in (torch.rand(20000, dim, generator=g, dtype=torch.float64) * 7 - 3, grid.reshape(-1, dim), flat):
+        lo, hi = c.min(0).values.contiguous(), c.max(0).values.contiguous()
+        bits = 63 // dim
+        host = morton_keys(c, lo, hi, bits)
+        dev = morton_keys(c.to(DEV), lo.to(DEV), hi.to(DEV), bits)
+        assert torch.equal(dev.cpu(), host)
+        assert torch.equal(morton_parts(c.to(DEV), 64).cpu(), morton_parts(c, 64))
