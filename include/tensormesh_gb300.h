@@ -237,7 +237,8 @@ int tm_quadrature_points(int32_t element, int32_t dtype, int32_t n_quad, const d
  * reference, whose K.solve has only Jacobi): z = C r + (I - C K) S (I - K C) r
  * with C = P K_c^-1 P^T (P piecewise constant over nc aggregates) and
  * S = diag(sw).  float32 inside; r and z are FP64 device vectors of length n.
- * work: float32 scratch of 2 n + 4 nc values.  Graph-capturable (no host
+ * work: float32 scratch of 2 n + 4 nc values (16-byte aligned for the fastest
+ * coarse matvecs).  Graph-capturable (no host
  * synchronisation, no allocation).
  */
 typedef struct tm_twolevel {
@@ -264,6 +265,12 @@ typedef struct tm_twolevel {
   const float* k_sval;
   int32_t k_narrow;
   int32_t pad1;
+  /* optional half-precision copy of K_c^-1 for the coarse matvecs: kc_half
+   * [nc*nc] IEEE binary16 H_ij = K_c^-1_ij / (kc_scale_i kc_scale_j) with
+   * kc_scale_i = sqrt(K_c^-1_ii) (|H_ij| <= 1, symmetric), kc_scale [nc]
+   * float32; NULL kc_half = the float32 kc_inv above */
+  const void* kc_half;
+  const float* kc_scale;
 } tm_twolevel;
 
 int tm_twolevel_apply(const tm_twolevel* t, const double* r, double* z, void* stream);

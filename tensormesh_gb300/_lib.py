@@ -70,6 +70,7 @@ class TwoLevel(ctypes.Structure):
         ("k_nnz", ctypes.c_int64), ("k_indptr", P), ("k_indices", P), ("k_values", P),
         ("sw", P), ("work", P),
         ("k_slice_ptr", P), ("k_scol", P), ("k_sval", P), ("k_narrow", ctypes.c_int32), ("pad1", ctypes.c_int32),
+        ("kc_half", P), ("kc_scale", P),
     ]
 
 

@@ -6,7 +6,9 @@
 //     z    = P (y_c - y_c2) + s                = C r + (I - C K) S (I - K C) r
 // P is piecewise constant over aggregates; P^T is a per-aggregate sum (one warp
 // per aggregate, fixed lane order and shuffle tree, so the result is
-// deterministic); K_c^-1 is a dense float32 matrix (one warp per row).
+// deterministic); K_c^-1 is a dense matrix (one warp per row), float32 or
+// its half-precision unit-diagonal form with a float32 diagonal scale.
+#include <cuda_fp16.h>
 #include "spmv.cuh"
 #include "../../include/tensormesh_gb300.h"
 
@@ -20,11 +22,12 @@ constexpr int kThreads = 256;
 // on them.
 constexpr int kTlIlp = 8;
 
-// rc[c] = sum of r over aggregate c: lane l adds entries l, l + 32, ... of
-// the aggregate in that order, then a shuffle tree (deterministic).
+// rc[c] = sum of r over aggregate c (times scale[c] when scale is given):
+// lane l adds entries l, l + 32, ... of the aggregate in that order, then a
+// shuffle tree (deterministic).
 template <class T>
 __global__ void restrict_kernel(int32_t nc, const int64_t* __restrict__ ptr, const int32_t* __restrict__ perm,
-                                const T* __restrict__ r, float* __restrict__ rc) {
+                                const T* __restrict__ r, const float* __restrict__ scale, float* __restrict__ rc) {
   const int c = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (c >= nc) return;  // the whole warp leaves together
@@ -43,7 +46,7 @@ __global__ void restrict_kernel(int32_t nc, const int64_t* __restrict__ ptr, con
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) rc[c] = s;
+  if (lane == 0) rc[c] = scale ? s * scale[c] : s;
 }
 
 // y = A x with A dense nc x nc (row-major), one warp per row.  kVec (nc a
@@ -96,6 +99,72 @@ inline void launch_gemv(int32_t nc, const float* A, const float* x, float* y, cu
   if (vec && vecx) gemv_kernel<true, true><<<grid, kThreads, 0, s>>>(nc, A, x, y);
   else if (vec) gemv_kernel<true, false><<<grid, kThreads, 0, s>>>(nc, A, x, y);
   else gemv_kernel<false, false><<<grid, kThreads, 0, s>>>(nc, A, x, y);
+}
+
+// y = D H D x with H the half-precision unit-diagonal form of K_c^-1 and
+// D = diag(scale): x arrives multiplied by D already (the restriction applies
+// it), so row i is y_i = scale_i sum_j H_ij x_j, one warp per row.  kVec (nc
+// a multiple of 8, H 16-byte aligned): eight halves per 16-byte load, lane l
+// taking octets l, l + 32, ...; kVecX: x is 16-byte aligned too.  Half the
+// bytes of the float32 matvec; the rounding of H (2^-11 of the diagonal
+// scale) left the flexible-CG iteration counts of the 128^3 C5 system
+// unchanged.
+template <bool kVec, bool kVecX>
+__global__ void gemv_half_kernel(int32_t nc, const __half* __restrict__ H, const float* __restrict__ scale,
+                                 const float* __restrict__ x, float* __restrict__ y) {
+  const int row = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= nc) return;
+  const __half* h = H + (int64_t)row * nc;
+  float s = 0.f;
+  if constexpr (kVec) {
+    const uint4* h8 = reinterpret_cast<const uint4*>(h);
+    const int n8 = nc >> 3;
+    for (int jb = lane; jb < n8; jb += 32 * kTlIlp) {
+      uint4 v[kTlIlp];
+#pragma unroll
+      for (int u = 0; u < kTlIlp; ++u) v[u] = jb + 32 * u < n8 ? __ldg(h8 + jb + 32 * u) : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+      for (int u = 0; u < kTlIlp; ++u) {
+        const int j = jb + 32 * u;
+        if (j < n8) {
+          float xv[8];
+          if constexpr (kVecX) {
+            const float4 a = __ldg(reinterpret_cast<const float4*>(x) + 2 * j);
+            const float4 b = __ldg(reinterpret_cast<const float4*>(x) + 2 * j + 1);
+            xv[0] = a.x; xv[1] = a.y; xv[2] = a.z; xv[3] = a.w;
+            xv[4] = b.x; xv[5] = b.y; xv[6] = b.z; xv[7] = b.w;
+          } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) xv[k] = __ldg(x + 8 * j + k);
+          }
+          const __half2* hv = reinterpret_cast<const __half2*>(&v[u]);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const float2 f = __half22float2(hv[k]);
+            s = fmaf(f.x, xv[2 * k], s);
+            s = fmaf(f.y, xv[2 * k + 1], s);
+          }
+        }
+      }
+    }
+  } else {
+    for (int j = lane; j < nc; j += 32) s = fmaf(__half2float(h[j]), x[j], s);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) y[row] = scale[row] * s;
+}
+
+inline void launch_gemv_half(int32_t nc, const void* H, const float* scale, const float* x, float* y,
+                             cudaStream_t s) {
+  const int grid = (nc + kThreads / 32 - 1) / (kThreads / 32);
+  const __half* h = static_cast<const __half*>(H);
+  const bool vec = (nc & 7) == 0 && ((uintptr_t)H & 15u) == 0;
+  const bool vecx = ((uintptr_t)x & 15u) == 0;
+  if (vec && vecx) gemv_half_kernel<true, true><<<grid, kThreads, 0, s>>>(nc, h, scale, x, y);
+  else if (vec) gemv_half_kernel<true, false><<<grid, kThreads, 0, s>>>(nc, h, scale, x, y);
+  else gemv_half_kernel<false, false><<<grid, kThreads, 0, s>>>(nc, h, scale, x, y);
 }
 
 __global__ void smooth_kernel(int64_t n, const int64_t* __restrict__ kp_ptr, const int32_t* __restrict__ kp_idx,
@@ -314,16 +383,21 @@ static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z,
   using namespace tmg::tl;
   const int64_t n = t->n;
   const int32_t nc = t->nc;
-  float* s1 = t->work;
-  float* r2 = s1 + n;
-  float* rc = r2 + n;
+  // the coarse vectors first, so that the matvec inputs rc and rc2 keep the
+  // scratch's alignment (16-byte loads when nc is even)
+  float* rc = t->work;
   float* yc = rc + nc;
   float* rc2 = yc + nc;
   float* yc2 = rc2 + nc;
+  float* s1 = yc2 + nc;
+  float* r2 = s1 + n;
   const int gc = (nc + kThreads / 32 - 1) / (kThreads / 32);
   const int gn = (int)((n + kThreads - 1) / kThreads);
-  restrict_kernel<double><<<gc, kThreads, 0, s>>>(nc, t->agg_ptr, t->agg_perm, r, rc);
-  launch_gemv(nc, t->kc_inv, rc, yc, s);
+  const bool half = t->kc_half != nullptr;
+  const float* rscale = half ? t->kc_scale : nullptr;
+  restrict_kernel<double><<<gc, kThreads, 0, s>>>(nc, t->agg_ptr, t->agg_perm, r, rscale, rc);
+  if (half) launch_gemv_half(nc, t->kc_half, t->kc_scale, rc, yc, s);
+  else launch_gemv(nc, t->kc_inv, rc, yc, s);
   smooth_kernel<<<gn, kThreads, 0, s>>>(n, t->kp_indptr, t->kp_indices, t->kp_values, yc, r, t->sw, s1);
   if (t->k_slice_ptr) {
     const int st = tm_spmv_sell(TM_F32, n, t->k_slice_ptr, t->k_narrow, t->k_scol, t->k_sval, s1, r2, s);
@@ -331,8 +405,9 @@ static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z,
   } else {
     tmg::launch_spmv<float>(n, t->k_nnz, t->k_indptr, t->k_indices, t->k_values, s1, r2, s);
   }
-  restrict_kernel<float><<<gc, kThreads, 0, s>>>(nc, t->agg_ptr, t->agg_perm, r2, rc2);
-  launch_gemv(nc, t->kc_inv, rc2, yc2, s);
+  restrict_kernel<float><<<gc, kThreads, 0, s>>>(nc, t->agg_ptr, t->agg_perm, r2, rscale, rc2);
+  if (half) launch_gemv_half(nc, t->kc_half, t->kc_scale, rc2, yc2, s);
+  else launch_gemv(nc, t->kc_inv, rc2, yc2, s);
   if (q_dot)
     finish_dot2_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, t->agg, yc, yc2, s1, r, q_dot, z, part);
   else
@@ -343,7 +418,7 @@ static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z,
 static bool twolevel_ok(const tm_twolevel* t) {
   return t->n >= 0 && t->nc >= 1 && t->k_nnz >= 0 && t->agg && t->agg_ptr && t->agg_perm && t->kc_inv &&
          t->kp_indptr && t->kp_indices && t->kp_values && t->k_indptr && t->k_indices && t->k_values && t->sw &&
-         t->work && (!t->k_slice_ptr || (t->k_scol && t->k_sval));
+         t->work && (!t->k_slice_ptr || (t->k_scol && t->k_sval)) && (!t->kc_half || t->kc_scale);
 }
 
 extern "C" int64_t tm_fcg_workspace_doubles(void) { return 2 * (int64_t)tmg::tl::kFcgBlocks + 8; }

@@ -232,6 +232,13 @@ class CoarseSpace:
         else:                                             # float32 not enough: factor in FP64
             Kinv = torch.cholesky_inverse(torch.linalg.cholesky(Ks))
         self.Kc_inv = (Kinv * s[:, None] * s[None, :]).float().contiguous()
+        # half-precision copy for the coarse matvecs of tm_twolevel_apply:
+        # H = D^-1 K_c^-1 D^-1 (symmetrised, unit diagonal, |H_ij| <= 1) with
+        # D = diag(sqrt(K_c^-1_ii)), half the bytes of the float32 matrix
+        d = torch.sqrt(torch.clamp(torch.diagonal(self.Kc_inv), min=torch.finfo(torch.float32).tiny))
+        H = 0.5 * (self.Kc_inv + self.Kc_inv.T) / d[:, None] / d[None, :]
+        self.kc_half = H.half().contiguous()
+        self.kc_scale = d.float().contiguous()
         self.agg_order = torch.argsort(agg, stable=True)
         self.agg_ptr = torch.zeros(nc + 1, dtype=torch.int64, device=dev)
         self.agg_ptr[1:] = torch.cumsum(torch.bincount(agg, minlength=nc), 0)
@@ -325,6 +332,7 @@ class LearnedPreconditioner:
         t.n, t.nc, t.pad0 = n, C.nc, 0
         t.agg, t.agg_ptr, t.agg_perm = C.agg32.data_ptr(), C.agg_ptr.data_ptr(), C.agg_order32.data_ptr()
         t.kc_inv = C.Kc_inv.data_ptr()
+        t.kc_half, t.kc_scale = C.kc_half.data_ptr(), C.kc_scale.data_ptr()
         t.kp_indptr, t.kp_indices, t.kp_values = (C.kp_indptr.data_ptr(), C.kp_indices.data_ptr(),
                                                   C.kp_values32.data_ptr())
         t.k_nnz = int(G.values32.shape[0])
