@@ -236,7 +236,7 @@ class CoarseSpace:
         # H = D^-1 K_c^-1 D^-1 (symmetrised, unit diagonal, |H_ij| <= 1) with
         # D = diag(sqrt(K_c^-1_ii)), half the bytes of the float32 matrix
         d = torch.sqrt(torch.clamp(torch.diagonal(self.Kc_inv), min=torch.finfo(torch.float32).tiny))
-        H = 0.5 * (self.Kc_inv + self.Kc_inv.T) / d[:, None] / d[None, :]
+        H = 0.5 * (self.Kc_inv + self.Kc_inv.T) / (d[:, None] * d[None, :])   # exactly symmetric
         self.kc_half = H.half().contiguous()
         self.kc_scale = d.float().contiguous()
         self.agg_order = torch.argsort(agg, stable=True)

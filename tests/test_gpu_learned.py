@@ -98,6 +98,37 @@ def test_two_level_preconditioner_is_symmetric_positive():
     assert float(torch.dot(u, pre(u))) > 0
 
 
+def test_two_level_apply_matches_a_torch_restatement():
+    """tm_twolevel_apply against the same operator written in torch float32,
+    with the coarse inverse as the kernels hold it (D H D, H in half
+    precision): y_c = K_c^-1 P^T r, s = S (r - K P y_c),
+    y_c2 = K_c^-1 P^T K s, z = P (y_c - y_c2) + s."""
+    K, f, coords = poisson_system(12, 4)
+    pre = LearnedPreconditioner(MPNN(DEV, seed=3), coarse_target=64)
+    pre.setup(K, coords)
+    C = pre.coarse
+    n = f.shape[0]
+    g = torch.Generator().manual_seed(11)
+    r = torch.randn(n, generator=g, dtype=torch.float64).to(DEV)
+    z = pre(r)
+    Kc = C.kc_scale[:, None] * C.kc_half.float() * C.kc_scale[None, :]
+
+    def coarse(v):
+        return Kc @ torch.zeros(C.nc, dtype=torch.float32, device=DEV).index_add_(0, C.agg, v.float())
+    kp = torch.sparse_csr_tensor(C.kp_indptr, C.kp_indices.long(), C.kp_values32, (n, C.nc))
+    Kf = torch.sparse_csr_tensor(K.indptr, K.indices.long(), K.values.float(), (n, n))
+    yc = coarse(r)
+    s1 = pre.sw.float() * (r.float() - kp @ yc)
+    yc2 = coarse(Kf @ s1)
+    ref = (yc - yc2)[C.agg] + s1
+    assert float((z.float() - ref).abs().max() / ref.abs().max()) <= 1e-4
+    # the half-precision H is the symmetric unit-diagonal form of the float32 inverse
+    H = C.kc_half.float()
+    assert torch.equal(H, H.T)
+    assert float((torch.diagonal(H) - 1).abs().max()) <= 1e-3
+    assert float((Kc - C.Kc_inv).abs().max() / C.Kc_inv.abs().max()) <= 1e-3
+
+
 def test_graph_replay_matches_eager_iterations():
     K, f, coords = poisson_system(12, 3)
     pre = LearnedPreconditioner(MPNN(DEV, seed=1), coarse_target=64)
