@@ -285,7 +285,8 @@ int tm_twolevel_apply(const tm_twolevel* t, const double* r, double* z, void* st
  * a_slice_ptr is non-NULL, its tm_sell_fill copy (a_slice_ptr, a_narrow,
  * a_scol, a_sval), M the two-level operator t.  x, r, p are
  * updated in place; q and z are scratch of n doubles; sc[0] holds rz on
- * entry and on exit (sc: 8 doubles: rz, alpha, beta, (p, q)); part is
+ * entry and on exit (sc: 8 doubles: rz, alpha, beta, (p, q), the rz of odd
+ * iterations, scratch); part is
  * scratch of tm_fcg_workspace_doubles() doubles.  Dot products reduce in a
  * fixed order (bitwise repeatable).  A non-positive (p, q) sets alpha = 0.
  */

@@ -219,46 +219,79 @@ __device__ __forceinline__ double fcg_sum_parts(const double* part, int nb) {
 }
 
 // part[b] = this CTA's share of (a, b)
+// The grid-stride loops below keep four iterations' loads in flight per
+// thread and consume them in index order, so every thread's sums are formed
+// in the same order as a one-at-a-time loop (the results do not depend on
+// the batching).
+constexpr int kFcgBatch = 4;
+
 __global__ void __launch_bounds__(kFcgThreads) fcg_dot_kernel(int64_t n, const double* __restrict__ a,
                                                                const double* __restrict__ b, double* part) {
   __shared__ double red[32];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   double v = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    v = fma(a[i], b[i], v);
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += kFcgBatch * stride) {
+    double av[kFcgBatch], bv[kFcgBatch];
+#pragma unroll
+    for (int u = 0; u < kFcgBatch; ++u) {
+      const int64_t i = i0 + u * stride;
+      av[u] = i < n ? a[i] : 0.0;
+      bv[u] = i < n ? b[i] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kFcgBatch; ++u)
+      if (i0 + u * stride < n) v = fma(av[u], bv[u], v);
+  }
   v = fcg_block_sum(v, red);
   if (threadIdx.x == 0) part[blockIdx.x] = v;
 }
 
-// alpha = rz / (p, q) (0 when (p, q) <= 0: the iteration then stands still
-// and the host's stagnation test takes over)
-__global__ void fcg_alpha_kernel(const double* part, int nb, double* sc) {
-  const double pq = fcg_sum_parts(part, nb);
-  if (threadIdx.x == 0) {
-    sc[3] = pq;
-    sc[1] = pq > 0.0 ? sc[0] / pq : 0.0;
-  }
-}
+// Scalars of iteration k: rz in sc[0] (k even) or sc[4] (k odd), so that the
+// kernel that forms the next rz never overwrites the one its other CTAs are
+// reading; alpha in sc[1], beta in sc[2], (p, q) in sc[3].
+__device__ __forceinline__ int fcg_rz_slot(int parity) { return parity ? 4 : 0; }
 
+// alpha = rz / (p, q) from the partials of (p, q) (every CTA sums them in
+// the same order; 0 when (p, q) <= 0: the iteration then stands still and
+// the host's stagnation test takes over), then x += alpha p, r -= alpha q
 __global__ void __launch_bounds__(kFcgThreads) fcg_xr_kernel(int64_t n, double* __restrict__ x,
                                                               double* __restrict__ r, const double* __restrict__ p,
-                                                              const double* __restrict__ q, const double* sc) {
-  const double alpha = sc[1];
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i] = fma(alpha, p[i], x[i]);
-    r[i] = fma(-alpha, q[i], r[i]);
+                                                              const double* __restrict__ q, const double* part,
+                                                              int nb, double* sc, int parity) {
+  __shared__ double s_alpha;
+  if (threadIdx.x < 32) {
+    const double pq = fcg_sum_parts(part, nb);
+    if (threadIdx.x == 0) {
+      const double al = pq > 0.0 ? sc[fcg_rz_slot(parity)] / pq : 0.0;
+      s_alpha = al;
+      if (blockIdx.x == 0) {
+        sc[1] = al;
+        sc[3] = pq;
+      }
+    }
   }
-}
-
-// Polak-Ribiere: beta = max(0, (z, r_new - r_old) / rz_old) with
-// r_new - r_old = -alpha q; then rz = (r_new, z)
-__global__ void fcg_beta_kernel(const double* part, int nb, double* sc) {
-  const double rzn = fcg_sum_parts(part, nb);
-  const double zq = fcg_sum_parts(part + nb, nb);
-  if (threadIdx.x == 0) {
-    const double rz = sc[0];
-    const double b = rz != 0.0 ? -sc[1] * zq / rz : 0.0;
-    sc[2] = b > 0.0 ? b : 0.0;
-    sc[0] = rzn;
+  __syncthreads();
+  const double alpha = s_alpha;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += kFcgBatch * stride) {
+    double xv[kFcgBatch], rv[kFcgBatch], pv[kFcgBatch], qv[kFcgBatch];
+#pragma unroll
+    for (int u = 0; u < kFcgBatch; ++u) {
+      const int64_t i = i0 + u * stride;
+      const bool ok = i < n;
+      xv[u] = ok ? x[i] : 0.0;
+      rv[u] = ok ? r[i] : 0.0;
+      pv[u] = ok ? p[i] : 0.0;
+      qv[u] = ok ? q[i] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kFcgBatch; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i < n) {
+        x[i] = fma(alpha, pv[u], xv[u]);
+        r[i] = fma(-alpha, qv[u], rv[u]);
+      }
+    }
   }
 }
 
@@ -273,13 +306,37 @@ __global__ void __launch_bounds__(kFcgThreads) finish_dot2_kernel(int64_t n, con
                                                                    const double* __restrict__ q,
                                                                    double* __restrict__ z, double* part) {
   __shared__ double red[32];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   double a = 0.0, c = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int g = agg[i];
-    const double zi = (double)((yc[g] - yc2[g]) + s1[i]);
-    z[i] = zi;
-    a = fma(r[i], zi, a);
-    c = fma(zi, q[i], c);
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += kFcgBatch * stride) {
+    int g[kFcgBatch];
+    float sv[kFcgBatch];
+    double rv[kFcgBatch], qv[kFcgBatch];
+#pragma unroll
+    for (int u = 0; u < kFcgBatch; ++u) {
+      const int64_t i = i0 + u * stride;
+      const bool ok = i < n;
+      g[u] = ok ? agg[i] : 0;
+      sv[u] = ok ? s1[i] : 0.f;
+      rv[u] = ok ? r[i] : 0.0;
+      qv[u] = ok ? q[i] : 0.0;
+    }
+    float y1[kFcgBatch], y2[kFcgBatch];
+#pragma unroll
+    for (int u = 0; u < kFcgBatch; ++u) {
+      y1[u] = yc[g[u]];
+      y2[u] = yc2[g[u]];
+    }
+#pragma unroll
+    for (int u = 0; u < kFcgBatch; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i < n) {
+        const double zi = (double)((y1[u] - y2[u]) + sv[u]);
+        z[i] = zi;
+        a = fma(rv[u], zi, a);
+        c = fma(zi, qv[u], c);
+      }
+    }
   }
   a = fcg_block_sum(a, red);
   c = fcg_block_sum(c, red);
@@ -289,11 +346,56 @@ __global__ void __launch_bounds__(kFcgThreads) finish_dot2_kernel(int64_t n, con
   }
 }
 
+// Polak-Ribiere beta = max(0, (z, r_new - r_old) / rz_old) with r_new - r_old
+// = -alpha q, from the partials of (r, z) and (z, q) (every CTA sums them in
+// the same order); rz_new = (r, z) goes to the other rz slot; then
+// p = z + beta p
 __global__ void __launch_bounds__(kFcgThreads) fcg_p_kernel(int64_t n, double* __restrict__ p,
-                                                             const double* __restrict__ z, const double* sc) {
-  const double beta = sc[2];
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = fma(beta, p[i], z[i]);
+                                                             const double* __restrict__ z, const double* part,
+                                                             int nb, double* sc, int parity) {
+  __shared__ double s_beta;
+  if (threadIdx.x < 32) {
+    const double rzn = fcg_sum_parts(part, nb);
+    const double zq = fcg_sum_parts(part + nb, nb);
+    if (threadIdx.x == 0) {
+      const double rz = sc[fcg_rz_slot(parity)];
+      const double b = rz != 0.0 ? -sc[1] * zq / rz : 0.0;
+      s_beta = b > 0.0 ? b : 0.0;
+      if (blockIdx.x == 0) {
+        sc[2] = s_beta;
+        sc[fcg_rz_slot(parity ^ 1)] = rzn;
+      }
+    }
+  }
+  __syncthreads();
+  const double beta = s_beta;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += kFcgBatch * stride) {
+    double pv[kFcgBatch], zv[kFcgBatch];
+#pragma unroll
+    for (int u = 0; u < kFcgBatch; ++u) {
+      const int64_t i = i0 + u * stride;
+      pv[u] = i < n ? p[i] : 0.0;
+      zv[u] = i < n ? z[i] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kFcgBatch; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i < n) p[i] = fma(beta, pv[u], zv[u]);
+    }
+  }
+}
+
+// rz of the last iteration back to sc[0] (after an odd number of iterations)
+__global__ void fcg_rz_home_kernel(double* sc) { sc[0] = sc[4]; }
+
+// CTAs of the flexible CG's vector kernels: two per SM for large systems,
+// fewer for small ones (four rows per thread at least), so that the per-CTA
+// partial sums every CTA adds up stay few; a function of n alone, so the
+// iteration stays bitwise repeatable.
+inline int fcg_blocks(int64_t n) {
+  const int64_t want = (n + (int64_t)kFcgThreads * kFcgBatch - 1) / ((int64_t)kFcgThreads * kFcgBatch);
+  return (int)(want < 1 ? 1 : (want > kFcgBlocks ? kFcgBlocks : want));
 }
 
 // ---- K P (the thin matrix of the coarse space) without a global sort -------
@@ -377,9 +479,9 @@ extern "C" int tm_kp_fill(int64_t n, const int64_t* indptr, const int32_t* indic
 }
 
 // z = M r.  With q_dot and part (the flexible CG), the last step also forms
-// the partial sums of (r, z) and (z, q_dot) for fcg_beta_kernel.
+// the partial sums of (r, z) and (z, q_dot) for fcg_p_kernel.
 static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z, cudaStream_t s,
-                               const double* q_dot = nullptr, double* part = nullptr) {
+                               const double* q_dot = nullptr, double* part = nullptr, int nb = 0) {
   using namespace tmg::tl;
   const int64_t n = t->n;
   const int32_t nc = t->nc;
@@ -409,7 +511,7 @@ static int twolevel_apply_impl(const tm_twolevel* t, const double* r, double* z,
   if (half) launch_gemv_half(nc, t->kc_half, t->kc_scale, rc2, yc2, s);
   else launch_gemv(nc, t->kc_inv, rc2, yc2, s);
   if (q_dot)
-    finish_dot2_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, t->agg, yc, yc2, s1, r, q_dot, z, part);
+    finish_dot2_kernel<<<nb, kFcgThreads, 0, s>>>(n, t->agg, yc, yc2, s1, r, q_dot, z, part);
   else
     finish_kernel<<<gn, kThreads, 0, s>>>(n, t->agg, yc, yc2, s1, z);
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
@@ -436,6 +538,7 @@ extern "C" int tm_fcg_twolevel_iterations(const tm_twolevel* t, int64_t a_nnz, c
   const int64_t n = t->n;
   if (n == 0 || iters == 0) return TM_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int nb = fcg_blocks(n);
   for (int it = 0; it < iters; ++it) {
     if (sell) {
       const int st = tm_spmv_sell(TM_F64, n, a_slice_ptr, a_narrow, a_scol, a_sval, p, q, stream);
@@ -443,14 +546,14 @@ extern "C" int tm_fcg_twolevel_iterations(const tm_twolevel* t, int64_t a_nnz, c
     } else {
       tmg::launch_spmv<double>(n, a_nnz, a_indptr, a_indices, a_values, p, q, s);
     }
-    fcg_dot_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, p, q, part);
-    fcg_alpha_kernel<<<1, 32, 0, s>>>(part, kFcgBlocks, sc);
-    fcg_xr_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, x, r, p, q, sc);
-    const int st = twolevel_apply_impl(t, r, z, s, q, part);
+    const int parity = it & 1;
+    fcg_dot_kernel<<<nb, kFcgThreads, 0, s>>>(n, p, q, part);
+    fcg_xr_kernel<<<nb, kFcgThreads, 0, s>>>(n, x, r, p, q, part, nb, sc, parity);
+    const int st = twolevel_apply_impl(t, r, z, s, q, part, nb);
     if (st != TM_OK) return st;
-    fcg_beta_kernel<<<1, 32, 0, s>>>(part, kFcgBlocks, sc);
-    fcg_p_kernel<<<kFcgBlocks, kFcgThreads, 0, s>>>(n, p, z, sc);
+    fcg_p_kernel<<<nb, kFcgThreads, 0, s>>>(n, p, z, part, nb, sc, parity);
   }
+  if (iters & 1) fcg_rz_home_kernel<<<1, 1, 0, s>>>(sc);
   return cudaPeekAtLastError() == cudaSuccess ? TM_OK : TM_ERR_CUDA;
 }
 
