@@ -172,3 +172,24 @@ def test_morton_parts_are_octree_cells():
         sel = pts[part == k] * 32
         ext = (sel.max(0).values - sel.min(0).values + 1).round().long()
         assert int(ext.prod()) == sel.shape[0]
+
+
+def test_morton_keys_interleave_the_quantised_coordinates():
+    """The host definition of the Z-order keys against a scalar restatement:
+    q_d = round-half-even((x_d - lo_d) / (hi_d - lo_d) * (2^bits - 1)), bit b
+    of q_d at key bit b D + d."""
+    from tensormesh_gb300.plan import morton_keys
+    g = torch.Generator().manual_seed(5)
+    for D in (2, 3):
+        c = torch.rand(300, D, generator=g, dtype=torch.float64) * 5 - 2
+        lo, hi = c.min(0).values, c.max(0).values
+        bits = 63 // D
+        got = morton_keys(c, lo, hi, bits).tolist()
+        scale = float((1 << bits) - 1)
+        for i in range(c.shape[0]):
+            key = 0
+            for d in range(D):
+                q = round(float((c[i, d] - lo[d]) / (hi[d] - lo[d])) * scale)   # Python round: half to even
+                for b in range(bits):
+                    key |= ((q >> b) & 1) << (b * D + d)
+            assert got[i] == key
