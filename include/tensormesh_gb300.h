@@ -351,7 +351,8 @@ int tm_spmv_csr(int32_t dtype, int64_t n_rows, int64_t nnz, const int64_t* indpt
  * 130-248 bicgstab_py).  Stops when ||r|| <= max(rtol*||b||, atol) on the
  * recurrence residual or after maxiter iterations.  x holds the initial guess
  * on entry.  work: caller-owned device scratch of at least
- * tm_pcg_workspace_bytes(dtype, n, nnz, tm_pcg_max_blocks(dtype)) bytes.
+ * tm_pcg_workspace_bytes(dtype, n, nnz, tm_pcg_max_blocks(dtype)) bytes
+ * (-TM_ERR_INVALID for a negative size or an unknown dtype).
  * FP64 systems are iterated in double-float arithmetic on the FP32 pipe
  * (values and vectors held as float pairs in the workspace).
  * Statuses of the solve itself are read back with tm_pcg_result.

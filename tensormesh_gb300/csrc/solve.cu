@@ -447,6 +447,7 @@ __global__ void scatter_kernel(int64_t n, const int64_t* __restrict__ map, const
 }  // namespace tmg
 
 extern "C" int64_t tm_pcg_workspace_bytes(int32_t dtype, int64_t n, int64_t nnz, int32_t max_blocks) {
+  if (n < 0 || nnz < 0 || max_blocks < 0 || (dtype != TM_F32 && dtype != TM_F64)) return -TM_ERR_INVALID;
   if (dtype == TM_F64)  // state | 7 df64 vectors | df64 values | double partials
     return 256 + 8 * (7 * n + nnz + 3 * (int64_t)max_blocks);
   // state | dinv r z p0 p1 q (6n) | partials (3 * blocks)
@@ -553,6 +554,7 @@ extern "C" int tm_pcg_result(const void* work, int32_t* iters, double* res, doub
 
 extern "C" int tm_csr_diagonal_inverse(int32_t dtype, int64_t n, const int64_t* indptr, const int32_t* indices,
                                        const void* values, void* out, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   if (!indptr || !indices || !values || !out) return TM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -567,6 +569,7 @@ extern "C" int tm_csr_diagonal_inverse(int32_t dtype, int64_t n, const int64_t* 
 }
 
 extern "C" int tm_gather(int32_t dtype, int64_t n, const int64_t* map, const void* src, void* dst, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   if (!map || !src || !dst) return TM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -581,6 +584,7 @@ extern "C" int tm_gather(int32_t dtype, int64_t n, const int64_t* map, const voi
 }
 
 extern "C" int tm_scatter(int32_t dtype, int64_t n, const int64_t* map, const void* src, void* dst, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   if (!map || !src || !dst) return TM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -597,6 +601,7 @@ extern "C" int tm_scatter(int32_t dtype, int64_t n, const int64_t* map, const vo
 extern "C" int tm_condense_rhs(int32_t dtype, int64_t n_inner, const int64_t* inner_dof, const void* rhs,
                                const int64_t* io_indptr, const int32_t* io_indices, const void* io_values,
                                const void* u_outer, void* out, void* stream) {
+  if (n_inner < 0) return TM_ERR_INVALID;
   if (n_inner == 0) return TM_OK;
   if (!inner_dof || !rhs || !io_indptr || !out) return TM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
