@@ -399,6 +399,7 @@ static inline unsigned tiles_of(int64_t n) { return (unsigned)((n + tmg::mp::TIL
 
 extern "C" int tm_mpnn_input_fwd(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff,
                                  const float* x, const float* w, void* H0, float* y, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   if (!indptr || !indices || !aoff || !x || !w || !H0 || !y) return TM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -409,6 +410,7 @@ extern "C" int tm_mpnn_input_fwd(int64_t n, const int64_t* indptr, const int32_t
 extern "C" int tm_mpnn_layer_fwd(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff,
                                  const void* Hin, const void* Wt, const float* bias, void* Hout, int32_t relu,
                                  void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   if (!indptr || !indices || !aoff || !Hin || !Wt || !bias || !Hout) return TM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -420,6 +422,7 @@ extern "C" int tm_mpnn_layer_fwd(int64_t n, const int64_t* indptr, const int32_t
 extern "C" int tm_mpnn_readout_fwd(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff,
                                    const void* H, const float* wr, const float* scale, float* u, float* t,
                                    float* out, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   if (!indptr || !indices || !aoff || !H || !wr || !u || !t || !out) return TM_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -431,6 +434,7 @@ extern "C" int tm_mpnn_readout_fwd(int64_t n, const int64_t* indptr, const int32
 extern "C" int tm_mpnn_readout_bwd(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff,
                                    const void* H, const float* g, const float* wr, float* dH, float* part,
                                    float* dwr, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const unsigned nt = tiles_of(n);
@@ -443,6 +447,7 @@ extern "C" int tm_mpnn_layer_bwd(int64_t n, const int64_t* indptr, const int32_t
                                  const void* Hin, const void* Hout, const float* dHout, const void* W, int32_t relu,
                                  float* part_dW, float* part_db, float* U, float* T, float* dHin, float* dW,
                                  float* db, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const unsigned nt = tiles_of(n);
@@ -458,6 +463,7 @@ extern "C" int tm_mpnn_layer_bwd(int64_t n, const int64_t* indptr, const int32_t
 
 extern "C" int tm_mpnn_input_bwd(int64_t n, const float* x, const float* y, const void* H0, const float* dH0,
                                  float* part, float* dw, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const unsigned nt = tiles_of(n);
@@ -468,6 +474,7 @@ extern "C" int tm_mpnn_input_bwd(int64_t n, const float* x, const float* y, cons
 
 extern "C" int tm_gather_axpy_f32(int64_t n, const int64_t* indptr, const int32_t* indices, const float* aoff,
                                   const float* u, const float* t, const float* scale, float* out, void* stream) {
+  if (n < 0) return TM_ERR_INVALID;
   if (n == 0) return TM_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   tmg::mp::gather_axpy<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, indptr, indices, aoff, u, t, scale, out);

@@ -60,3 +60,8 @@ def test_null_pointers_unknown_dtypes_and_flags_are_rejected(lib):
     t = _lib.TwoLevel()
     t.n, t.nc = 10, 0                                                            # no aggregates
     assert lib.tm_twolevel_apply(t, FAKE, FAKE, None) == INV
+
+
+def test_network_entries_reject_negative_sizes(lib):
+    assert lib.tm_mpnn_input_fwd(-1, FAKE, FAKE, FAKE, FAKE, FAKE, FAKE, FAKE, None) == INV
+    assert lib.tm_gather_axpy_f32(-1, FAKE, FAKE, FAKE, FAKE, FAKE, FAKE, FAKE, None) == INV
