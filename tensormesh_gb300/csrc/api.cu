@@ -136,7 +136,7 @@ extern "C" int tm_quadrature_points(int32_t element, int32_t dtype, int32_t n_qu
                                     void* out, void* stream) {
   const int B = tmg::n_basis(element);
   if (B < 0) return TM_ERR_UNSUPPORTED;
-  if (!tables || !points || !elements || !out || n_quad < 1 || n_quad > 11) return TM_ERR_INVALID;
+  if (!tables || !points || !elements || !out || n_quad < 1 || n_quad > 11 || n_elements < 0) return TM_ERR_INVALID;
   if (n_elements == 0) return TM_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int64_t total = n_elements * n_quad;
