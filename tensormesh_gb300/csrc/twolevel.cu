@@ -186,10 +186,10 @@ __global__ void finish_kernel(int64_t n, const int32_t* __restrict__ agg, const 
 }
 
 // ---- flexible CG with the two-level preconditioner, vector work fused ----
-// Scalars live on the device (no host round trip per iteration): sc[0] = rz
-// = (r, z), sc[1] = alpha, sc[2] = beta, sc[3] = (p, q).  Dot products
-// reduce per CTA (fixed tree) into part[], then one CTA sums part[] in a
-// fixed order, so every iteration is bitwise repeatable.
+// Scalars live on the device (no host round trip per iteration; slots below
+// at fcg_rz_slot).  Dot products reduce per CTA (fixed tree) into part[];
+// the kernel that needs the scalar sums part[] in one fixed order in every
+// CTA, so every iteration is bitwise repeatable.
 constexpr int kFcgThreads = 512;
 constexpr int kFcgBlocks = 304;
 
@@ -218,13 +218,13 @@ __device__ __forceinline__ double fcg_sum_parts(const double* part, int nb) {
   return v;  // valid in lane 0
 }
 
-// part[b] = this CTA's share of (a, b)
 // The grid-stride loops below keep four iterations' loads in flight per
 // thread and consume them in index order, so every thread's sums are formed
 // in the same order as a one-at-a-time loop (the results do not depend on
 // the batching).
 constexpr int kFcgBatch = 4;
 
+// part[b] = this CTA's share of (a, b)
 __global__ void __launch_bounds__(kFcgThreads) fcg_dot_kernel(int64_t n, const double* __restrict__ a,
                                                                const double* __restrict__ b, double* part) {
   __shared__ double red[32];
