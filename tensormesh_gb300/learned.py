@@ -186,8 +186,9 @@ class CoarseSpace:
     (n x n_c, a few entries per row: only rows next to an aggregate border
     have more than one), and K_c^-1 = (P^T K P)^-1, inverted once after a
     symmetric diagonal scaling (Cholesky in float32, in FP64 if float32 is not
-    positive definite) and kept in float32 for the matvec; the preconditioner
-    only needs it approximately."""
+    positive definite) and kept in float32 (the torch path) and as a
+    half-precision unit-diagonal matrix with a float32 diagonal scale (the
+    kernels' matvecs); the preconditioner only needs it approximately."""
 
     def __init__(self, indptr, indices, values, coords, target: int = 512):
         from .adjoint import segment_sum
